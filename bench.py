@@ -1,0 +1,298 @@
+"""Benchmark of the per-pixel Mandelbrot path on GB300.
+
+Workload (one step): the 1920x1080 view with 4x4 multisampling (33,177,600
+samples) at -0.743643887037151+0.131825904205330i, width 1e-12, N 50,000,
+series tolerance 1e-10 -- rendered by the FP32-floatexp perturbation kernel,
+with the plain FP64 perturbation kernel measured beside it on the same
+precomputed orbit.  The metric is pixel-iterations per second: the sum of
+the samples' escape counts (series-skipped iterations included, interior
+samples counted as N) over the render time.
+
+`value`  : device time of the render kernel, inputs resident, L2 flushed
+           between steps.
+`e2e`    : the same through the C ABI with host buffers: upload of the step's
+           tables, render, multisample reduce, copy of the reduced grid to host.
+--impl reference : the reference algorithm (the oracle's restatement of
+           mandelbrot.cpp, arbitrary-precision continuation) on the host cores.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CENTER = ("-0.743643887037151", "0.131825904205330")
+WIDTH = "1e-12"
+NR, NC, SC, N_ITER, TOL = 1080, 1920, 4, 50000, 1e-10
+METRIC = "pixel-iters/s on 1 GB300: FP32-floatexp vs plain FP64, >=99.99% px exact iter"
+# Algorithmic flops of one perturbation step (t = 2Z + d: 2 add; t*d: 4 mul
+# 2 add; + eps: 2 add; Y = Z + d: 2 add; |Y|^2: 2 mul 1 add; |d|^2: 2 mul 1 add).
+FLOPS_PER_ITER = 18
+
+
+def step_string():
+    from decimal import Decimal, getcontext
+    getcontext().prec = 40
+    return str(Decimal(WIDTH) / Decimal(NC))
+
+
+def workload_config():
+    return {"workload": "newman C2 view 1920x1080 x 4x4 samples, width 1e-12, N 50000",
+            "center": "%s%+si" % (CENTER[0], CENTER[1].lstrip("+")), "rows": NR, "cols": NC,
+            "multisample": SC, "samples": NR * NC * SC * SC, "max_iter": N_ITER,
+            "sa_tolerance": TOL, "l2": "flushed (256 MB write) between timed steps"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for k, n in enumerate(names):
+                if p[5 + k].lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_reference(seconds, threads, seed=7):
+    """The reference algorithm on the host: getIterations with its
+    arbitrary-precision continuation, on a seeded random sample of the
+    workload's samples until `seconds` of work is done.  Returns
+    (pixel-iters/s, samples, threads)."""
+    from oracle import oracle
+    o = oracle.OracleView(NR, NC)
+    o.set_view(CENTER[0], CENTER[1], step_string(), step_string(), N_ITER, TOL)
+    o.scale_up(SC)
+    o.precompute(threads=threads)
+    rng = np.random.default_rng(seed)
+    nr, nc = o.rows, o.cols
+    total_it, total_px, elapsed = 0, 0, 0.0
+    batch = max(16, 8 * threads)
+    while elapsed < seconds:
+        k = rng.choice(nr * nc, size=batch, replace=False)
+        t0 = time.perf_counter()
+        it, _ = o.render_pixels(k // nc, k % nc, oracle.MODE_REF, threads=threads)
+        elapsed += time.perf_counter() - t0
+        total_it += int(it.astype(np.int64).sum())
+        total_px += batch
+    return total_it / elapsed, total_px, threads
+
+
+def run_reference(args):
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    value, px, cores = cpu_reference(min(20.0, 4.0 * max(1, args.steps)), threads)
+    line = {"metric": METRIC, "value": value, "unit": "pixel-iters/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "mpf",
+            "data": "synthetic view (no dataset)", "config": workload_config(),
+            "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": "pixel-iters/s", "cores": cores,
+                             "kind": "port",
+                             "sample": "%d random samples of the 33,177,600, reference "
+                                       "getIterations (MP continuation)" % px},
+            "e2e": {"value": value, "unit": "pixel-iters/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    import newman_gb300 as nm
+
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    step = step_string()
+    stream = torch.cuda.Stream()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def make(path):
+        m = nm.Mandelbrot(NR, NC)
+        m.set_view(CENTER[0], CENTER[1], step, step, N_ITER, TOL)
+        m.scaleUp(SC)
+        m.set_path(path)
+        return m
+
+    primary = nm.PATH_FE32 if args.path == "fe32" else nm.PATH_FP64
+    m = make(primary)
+    t0 = time.perf_counter()
+    m.precompute()
+    precompute_s = time.perf_counter() - t0
+    m.upload()
+
+    def render_timed(mm, k, w):
+        times = []
+        for i in range(w + k):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                mm.render_rows(0, mm.rows(), stream.cuda_stream)
+                e1.record(stream)
+            stream.synchronize()
+            if i >= w:
+                times.append(e0.elapsed_time(e1))
+        return times
+
+    render_timed(m, 0, args.warmup)
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        wall0 = time.perf_counter()
+        times = render_timed(m, args.steps, 0)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+    barrier()
+    ms = float(np.mean(times))
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    g = m.grid()
+    eff_iters = int(g["iterations"].astype(np.int64).sum())
+    executed = m.stat(nm.STAT_EXECUTED_ITERS)
+    value = eff_iters * world / (ms * 1e-3)
+
+    # e2e through the C ABI with host buffers
+    red = np.empty((NR, NC), nm.ESCAPE_DTYPE)
+    e2e_times = []
+    for i in range(1 + args.steps):
+        t0 = time.perf_counter()
+        m.upload()
+        m.render()
+        m.reduce(SC, red)
+        if i:
+            e2e_times.append(time.perf_counter() - t0)
+    e2e_s = float(np.mean(e2e_times))
+    n_sample = NR * SC * NC * SC
+    h2d = 16 * (NC * SC + NR * SC) + 8 * (NC * SC + NR * SC)
+    xlen = m.stat(nm.STAT_ORBIT_LENGTH)
+    h2d += xlen * 16 * 6 + xlen * 8 + (xlen + 2) * 16
+
+    line = None
+    if rank == 0:
+        peak32 = nm.peak_flops(0)
+        peak64 = nm.peak_flops(2)
+        peak = peak32 if primary == nm.PATH_FE32 else peak64
+        achieved = executed * FLOPS_PER_ITER / (ms * 1e-3)
+        line = {
+            "metric": METRIC, "value": value, "unit": "pixel-iters/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp32+int-exponent" if primary == nm.PATH_FE32 else "fp64",
+            "data": "synthetic view (no dataset)", "config": workload_config(),
+            "path": args.path,
+            "executed_iters_per_step": executed, "effective_iters_per_step": eff_iters,
+            "precompute_s": precompute_s, "wall_s": wall,
+            "gpu_launches": 2 * args.steps,
+            "roofline": {"bound": "fp32" if primary == nm.PATH_FE32 else "fp64",
+                         "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
+                         "frac": achieved / peak, "traffic": None,
+                         "peak_source": "measured by nm_peak_flops on this GPU"},
+            "clocks": clocks.summary(),
+            "e2e": {"value": eff_iters / e2e_s, "unit": "pixel-iters/s",
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": NR * NC * 8},
+        }
+        if not args.no_cpu:
+            v, px, cores = cpu_reference(args.cpu_seconds, 1)
+            line["cpu_baseline"] = {"value": v, "unit": "pixel-iters/s", "cores": cores,
+                                    "kind": "port",
+                                    "sample": "%d random samples of the 33,177,600, reference "
+                                              "getIterations (MP continuation), 1 thread" % px}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--path", default="fe32", choices=["fe32", "fp64"])
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,159 @@
+/*
+ * newman_gb300 -- C ABI of the GPU per-pixel Mandelbrot path.
+ *
+ * One `nm_handle` stands in for one object of the reference's C++ class
+ * `Mandelbrot` (mandelbrot.h:7-53 of axnjaxn/newman): it owns the view (center,
+ * pixel step, iteration count, series tolerance, arbitrary precision), the
+ * precomputed reference orbit and series, and the output grid -- a row-major
+ * array of {int32 iterations, float smoothing} samples, index r*nc + c, the
+ * layout of the reference's RenderGrid (grid.h:6-25).  The grid lives in GPU
+ * memory and is copied out on request.
+ *
+ * Every call returns an int status (NM_OK = 0) unless stated otherwise; the
+ * message of the last failure on the calling thread is nm_last_error().  A
+ * handle is used by one thread at a time (nm_cancel excepted); separate
+ * handles are independent.  Views are exchanged as decimal strings, the
+ * format of the reference's save files (viewer.cpp:12-23).
+ */
+#ifndef NEWMAN_GB300_H
+#define NEWMAN_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct nm_handle nm_handle;
+
+/* grid.h:8-14, RenderGrid::EscapeValue -- 8 bytes, same layout. */
+typedef struct {
+  int32_t iterations;
+  float smoothing;
+} nm_escape_value;
+
+enum nm_status {
+  NM_OK = 0,
+  NM_ERR_ARG = 1,        /* bad argument (size, index, N < 1, null pointer) */
+  NM_ERR_PARSE = 2,      /* a decimal string did not parse */
+  NM_ERR_STATE = 3,      /* call out of order, e.g. a deep render before nm_precompute */
+  NM_ERR_CUDA = 4,       /* CUDA runtime error (message in nm_last_error) */
+  NM_ERR_CANCELLED = 5,  /* nm_cancel stopped the render; the grid is partial */
+  NM_ERR_IO = 6,         /* file could not be opened / read */
+  NM_ERR_UNSUPPORTED = 7 /* option or path not available for this view */
+};
+
+/* Arithmetic of the per-sample work (nm_set_path). */
+enum nm_path {
+  /* The reference's choice: its double loop when useHardware() holds
+     (mandelbrot.cpp:231-259), else the plain FP64 perturbation path. */
+  NM_PATH_REFERENCE = 0,
+  /* Plain FP64 perturbation: series skip, then FP64 delta iteration. */
+  NM_PATH_FP64 = 1,
+  /* FP32 mantissa + int exponent delta iteration (floatexp). */
+  NM_PATH_FE32 = 2
+};
+
+enum nm_option {
+  NM_OPT_TILE_W = 0,      /* sample order: tile width (default 16) */
+  NM_OPT_TILE_H = 1,      /* tile height (default 16) */
+  NM_OPT_CHUNK = 2,       /* iterations between lane refills (default 32) */
+  NM_OPT_KEEP_SMOOTH64 = 3, /* 1: also keep the unrounded double smoothing */
+  NM_OPT_THREADS = 4,     /* host threads for the probe search (0 = all) */
+  NM_OPT_BLOCKS = 5,      /* persistent blocks (0 = fill the GPU) */
+  NM_OPT_RENORM = 6       /* FE32: steps between exponent renormalisations */
+};
+
+enum nm_stat {
+  NM_STAT_CARDIOID_UNDECIDED = 0, /* cardioid tests within 2^-96 of the boundary */
+  NM_STAT_EXECUTED_ITERS = 1,     /* z^2 + c steps run on the GPU in the last render */
+  NM_STAT_SAMPLES = 2,            /* samples finished in the last render */
+  NM_STAT_REBASES = 3,            /* perturbation rebases in the last render */
+  NM_STAT_GLITCHES = 4,           /* FE32 steps re-checked in FP64 */
+  NM_STAT_ORBIT_LENGTH = 16,      /* X.size() of the last precompute */
+  NM_STAT_PROBE_INDEX = 17,       /* winning probe of findProbe */
+  NM_STAT_PRECISION_BITS = 18,    /* arbitrary precision of the view */
+  NM_STAT_PRECOMPUTE_US = 19      /* host time of the last nm_precompute */
+};
+
+/* Mandelbrot::Mandelbrot(int nr, int nc), mandelbrot.cpp:8-17: center -0.5,
+   step 4/nc x 3/nr, N 256, tolerance 1e-10.  Binds to the current CUDA
+   device.  Returns NULL on failure (nm_last_error). */
+nm_handle* nm_create(int nr, int nc);
+/* Value copy (the reference copies Mandelbrot objects, viewer.cpp:193,251). */
+nm_handle* nm_copy(const nm_handle* src);
+void nm_destroy(nm_handle* h);
+const char* nm_last_error(void);
+
+/* Public fields N, error_tolerance, center, sz (mandelbrot.h:23-25).  The
+   step string fixes the precision (setPrecision, mandelbrot.cpp:37-56);
+   min_bits > 0 raises it.  Decimal strings as mpf_set_str reads them. */
+int nm_set_view(nm_handle* h, const char* center_re, const char* center_im, const char* step_re,
+                const char* step_im, int N, double tolerance, int min_bits);
+/* which: 0 center.re, 1 center.im, 2 sz.re, 3 sz.im.  Writes a decimal string. */
+int nm_get_view(const nm_handle* h, int which, char* buf, int buflen);
+int nm_set_iterations(nm_handle* h, int N);          /* Mandelbrot::N */
+int nm_get_iterations(const nm_handle* h);
+int nm_set_tolerance(nm_handle* h, double tolerance); /* Mandelbrot::error_tolerance */
+int nm_rows(const nm_handle* h);                       /* rows(), mandelbrot.h:33 */
+int nm_cols(const nm_handle* h);                       /* cols(), mandelbrot.h:34 */
+int nm_use_hardware(const nm_handle* h);               /* useHardware(), mandelbrot.cpp:256 */
+
+int nm_set_path(nm_handle* h, int path);               /* enum nm_path */
+int nm_set_option(nm_handle* h, int option, long long value);
+int nm_get_stat(nm_handle* h, int stat, long long* value);
+
+/* precompute(), mandelbrot.cpp:261-267: for deep views the probe search,
+   reference orbit and series coefficients, on host threads, and their upload. */
+int nm_precompute(nm_handle* h);
+/* Re-issue the host-to-device copy of the precomputed tables on the handle's
+   stream (asynchronous). */
+int nm_upload(nm_handle* h);
+
+/* computeRow(r), mandelbrot.cpp:269-283: render one row, synchronously. */
+int nm_compute_row(nm_handle* h, int r);
+/* Render rows [r0, r1) asynchronously on `stream` (a cudaStream_t; NULL =
+   the handle's own stream).  nm_synchronize waits and reports cancellation. */
+int nm_render_rows(nm_handle* h, int r0, int r1, void* stream);
+/* All rows, synchronously: the row loop of viewer.cpp:166-171. */
+int nm_render(nm_handle* h);
+int nm_synchronize(nm_handle* h);
+/* Stop the render in flight at the next sample hand-out (any thread); the
+   reference polls ESC between rows (viewer.cpp:126-155). */
+int nm_cancel(nm_handle* h);
+
+/* at(r, c), mandelbrot.cpp:318 */
+int nm_at(nm_handle* h, int r, int c, nm_escape_value* out);
+/* at(r, c, sc), mandelbrot.cpp:320-332: float mean of sc x sc samples */
+int nm_at_sc(nm_handle* h, int r, int c, int sc, nm_escape_value* out);
+/* scaleUp(sc) / scaleDown(sc), mandelbrot.cpp:334-360, on the GPU grid. */
+int nm_scale_up(nm_handle* h, int sc);
+int nm_scale_down(nm_handle* h, int sc);
+/* The whole scaleDown(sc) grid written to host memory, handle unchanged:
+   (rows/sc) x (cols/sc) values. */
+int nm_reduce(nm_handle* h, int sc, nm_escape_value* host_out);
+/* Copy the grid (rows x cols) to host memory. */
+int nm_get_grid(nm_handle* h, nm_escape_value* host_out);
+/* Copy the unrounded double smoothing (needs NM_OPT_KEEP_SMOOTH64). */
+int nm_get_smoothing64(nm_handle* h, double* host_out);
+/* Device pointers of the grid (valid until the next resize). */
+int nm_device_grid(nm_handle* h, nm_escape_value** grid, double** smooth64);
+
+/* pointAt(r, c, sc), mandelbrot.cpp:285-290, as two decimal strings. */
+int nm_point_at(const nm_handle* h, int r, int c, int sc, char* re, char* im, int buflen);
+int nm_translate(nm_handle* h, int dr, int dc, int sc);            /* mandelbrot.cpp:292-295 */
+int nm_zoom(nm_handle* h, float scale);                            /* mandelbrot.cpp:297-302 */
+int nm_zoom_at(nm_handle* h, float scale, int r, int c, int sc);   /* mandelbrot.cpp:304-316 */
+int nm_load_legacy(nm_handle* h, const char* path);                /* mandelbrot.cpp:19-35 */
+int nm_save(const nm_handle* h, const char* path);                 /* viewer.cpp:12-23 */
+
+/* Measured issue ceiling of the current GPU, in flop/s (no reference
+   counterpart; the roofline denominator of the per-sample kernels).
+   kind 0: FP32 FMA, 1: FP64 FMA, 2: FP64 unfused multiply + add. */
+int nm_peak_flops(int kind, double* flops_per_s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NEWMAN_GB300_H */

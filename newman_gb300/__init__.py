@@ -1,0 +1,295 @@
+"""newman_gb300: GPU per-pixel Mandelbrot path with the reference's interface.
+
+`Mandelbrot` mirrors the C++ class of axnjaxn/newman (mandelbrot.h:7-53) over
+the C ABI of include/newman_gb300.h: the same fields (N, error_tolerance,
+center, sz), the same calls (precompute, computeRow, at, scaleUp, scaleDown,
+pointAt, translate, zoom, zoomAt, loadLegacy) and the same grid of
+{int32 iterations, float smoothing} samples.  The per-sample work always runs
+in the CUDA library; if the library is missing, importing this module fails.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libnewman_gb300.so")
+
+# include/newman_gb300.h
+NM_OK, NM_ERR_ARG, NM_ERR_PARSE, NM_ERR_STATE, NM_ERR_CUDA, NM_ERR_CANCELLED, NM_ERR_IO, \
+    NM_ERR_UNSUPPORTED = range(8)
+PATH_REFERENCE, PATH_FP64, PATH_FE32 = 0, 1, 2
+OPT_TILE_W, OPT_TILE_H, OPT_CHUNK, OPT_KEEP_SMOOTH64, OPT_THREADS, OPT_BLOCKS, OPT_RENORM = range(7)
+STAT_CARDIOID_UNDECIDED, STAT_EXECUTED_ITERS, STAT_SAMPLES, STAT_REBASES, STAT_GLITCHES = range(5)
+STAT_ORBIT_LENGTH, STAT_PROBE_INDEX, STAT_PRECISION_BITS, STAT_PRECOMPUTE_US = 16, 17, 18, 19
+
+ESCAPE_DTYPE = np.dtype([("iterations", "<i4"), ("smoothing", "<f4")])
+
+# Every symbol include/newman_gb300.h declares.
+EXPORTS = (
+    "nm_create", "nm_copy", "nm_destroy", "nm_last_error", "nm_set_view", "nm_get_view",
+    "nm_set_iterations", "nm_get_iterations", "nm_set_tolerance", "nm_rows", "nm_cols",
+    "nm_use_hardware", "nm_set_path", "nm_set_option", "nm_get_stat", "nm_precompute",
+    "nm_upload", "nm_compute_row", "nm_render_rows", "nm_render", "nm_synchronize", "nm_cancel",
+    "nm_at", "nm_at_sc", "nm_scale_up", "nm_scale_down", "nm_reduce", "nm_get_grid",
+    "nm_get_smoothing64", "nm_device_grid", "nm_point_at", "nm_translate", "nm_zoom",
+    "nm_zoom_at", "nm_load_legacy", "nm_save", "nm_peak_flops",
+)
+
+
+class NewmanError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s (status %d)" % (msg, code))
+        self.code = code
+
+
+class EscapeValue(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int32), ("smoothing", ctypes.c_float)]
+
+
+_lib = None
+
+
+def load_library(path=LIB_PATH):
+    """Loads the CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError("newman_gb300 CUDA library not built (%s); run "
+                          "`python -c 'import __graft_entry__ as g; g.build()'`" % path)
+    L = ctypes.CDLL(path)
+    vp, i32, dbl, cp, ll = (ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_char_p,
+                            ctypes.c_longlong)
+    P = ctypes.POINTER
+    sig = {
+        "nm_create": (vp, [i32, i32]),
+        "nm_copy": (vp, [vp]),
+        "nm_destroy": (None, [vp]),
+        "nm_last_error": (cp, []),
+        "nm_set_view": (i32, [vp, cp, cp, cp, cp, i32, dbl, i32]),
+        "nm_get_view": (i32, [vp, i32, cp, i32]),
+        "nm_set_iterations": (i32, [vp, i32]),
+        "nm_get_iterations": (i32, [vp]),
+        "nm_set_tolerance": (i32, [vp, dbl]),
+        "nm_rows": (i32, [vp]),
+        "nm_cols": (i32, [vp]),
+        "nm_use_hardware": (i32, [vp]),
+        "nm_set_path": (i32, [vp, i32]),
+        "nm_set_option": (i32, [vp, i32, ll]),
+        "nm_get_stat": (i32, [vp, i32, P(ll)]),
+        "nm_precompute": (i32, [vp]),
+        "nm_upload": (i32, [vp]),
+        "nm_compute_row": (i32, [vp, i32]),
+        "nm_render_rows": (i32, [vp, i32, i32, vp]),
+        "nm_render": (i32, [vp]),
+        "nm_synchronize": (i32, [vp]),
+        "nm_cancel": (i32, [vp]),
+        "nm_at": (i32, [vp, i32, i32, P(EscapeValue)]),
+        "nm_at_sc": (i32, [vp, i32, i32, i32, P(EscapeValue)]),
+        "nm_scale_up": (i32, [vp, i32]),
+        "nm_scale_down": (i32, [vp, i32]),
+        "nm_reduce": (i32, [vp, i32, vp]),
+        "nm_get_grid": (i32, [vp, vp]),
+        "nm_get_smoothing64": (i32, [vp, vp]),
+        "nm_device_grid": (i32, [vp, P(vp), P(vp)]),
+        "nm_point_at": (i32, [vp, i32, i32, i32, cp, cp, i32]),
+        "nm_translate": (i32, [vp, i32, i32, i32]),
+        "nm_zoom": (i32, [vp, ctypes.c_float]),
+        "nm_zoom_at": (i32, [vp, ctypes.c_float, i32, i32, i32]),
+        "nm_load_legacy": (i32, [vp, cp]),
+        "nm_save": (i32, [vp, cp]),
+        "nm_peak_flops": (i32, [i32, P(dbl)]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def _check(rc):
+    if rc != NM_OK:
+        raise NewmanError(rc, _lib.nm_last_error().decode(errors="replace"))
+
+
+def _s(x):
+    return str(x).encode()
+
+
+def peak_flops(kind):
+    """Measured FP32 FMA (0), FP64 FMA (1) or FP64 unfused (2) flop/s."""
+    v = ctypes.c_double(0.0)
+    _check(load_library().nm_peak_flops(int(kind), ctypes.byref(v)))
+    return v.value
+
+
+class Mandelbrot:
+    """One reference `Mandelbrot` object (mandelbrot.h:7-53) on the GPU."""
+
+    def __init__(self, nr=1, nc=1, _handle=None):
+        L = load_library()
+        self._h = _handle if _handle is not None else L.nm_create(int(nr), int(nc))
+        if not self._h:
+            raise NewmanError(NM_ERR_ARG, L.nm_last_error().decode())
+
+    def __del__(self):
+        h, self._h = getattr(self, "_h", None), None
+        if h and _lib is not None:
+            _lib.nm_destroy(h)
+
+    def copy(self):
+        """Value copy (the reference assigns Mandelbrot objects, viewer.cpp:193)."""
+        h = _lib.nm_copy(self._h)
+        if not h:
+            raise NewmanError(NM_ERR_CUDA, _lib.nm_last_error().decode())
+        return Mandelbrot(_handle=h)
+
+    # ---- fields -----------------------------------------------------------
+    @property
+    def N(self):
+        return _lib.nm_get_iterations(self._h)
+
+    @N.setter
+    def N(self, value):
+        _check(_lib.nm_set_iterations(self._h, int(value)))
+
+    @property
+    def error_tolerance(self):
+        return self._tol if hasattr(self, "_tol") else 1e-10
+
+    @error_tolerance.setter
+    def error_tolerance(self, value):
+        _check(_lib.nm_set_tolerance(self._h, float(value)))
+        self._tol = float(value)
+
+    def _view(self, which):
+        buf = ctypes.create_string_buffer(1 << 16)
+        _check(_lib.nm_get_view(self._h, which, buf, len(buf)))
+        return buf.value.decode()
+
+    @property
+    def center(self):
+        return self._view(0), self._view(1)
+
+    @property
+    def sz(self):
+        return self._view(2), self._view(3)
+
+    def set_view(self, center_re, center_im, step_re, step_im=None, N=None, tolerance=None,
+                 min_bits=0):
+        """Sets center, pixel step (decimal strings), N and tolerance at once."""
+        step_im = step_re if step_im is None else step_im
+        N = self.N if N is None else N
+        tol = self.error_tolerance if tolerance is None else tolerance
+        _check(_lib.nm_set_view(self._h, _s(center_re), _s(center_im), _s(step_re), _s(step_im),
+                                int(N), float(tol), int(min_bits)))
+        self._tol = float(tol)
+
+    def rows(self):
+        return _lib.nm_rows(self._h)
+
+    def cols(self):
+        return _lib.nm_cols(self._h)
+
+    def useHardware(self):
+        return bool(_lib.nm_use_hardware(self._h))
+
+    def set_path(self, path):
+        _check(_lib.nm_set_path(self._h, int(path)))
+
+    def set_option(self, option, value):
+        _check(_lib.nm_set_option(self._h, int(option), int(value)))
+
+    def stat(self, which):
+        v = ctypes.c_longlong(0)
+        _check(_lib.nm_get_stat(self._h, int(which), ctypes.byref(v)))
+        return v.value
+
+    # ---- rendering ----------------------------------------------------------
+    def precompute(self):
+        _check(_lib.nm_precompute(self._h))
+
+    def upload(self):
+        _check(_lib.nm_upload(self._h))
+
+    def computeRow(self, r):
+        _check(_lib.nm_compute_row(self._h, int(r)))
+
+    def render_rows(self, r0, r1, stream=None):
+        _check(_lib.nm_render_rows(self._h, int(r0), int(r1), stream))
+
+    def render(self):
+        _check(_lib.nm_render(self._h))
+
+    def synchronize(self):
+        _check(_lib.nm_synchronize(self._h))
+
+    def cancel(self):
+        _check(_lib.nm_cancel(self._h))
+
+    # ---- grid ----------------------------------------------------------------
+    def at(self, r, c, sc=None):
+        e = EscapeValue()
+        if sc is None:
+            _check(_lib.nm_at(self._h, int(r), int(c), ctypes.byref(e)))
+        else:
+            _check(_lib.nm_at_sc(self._h, int(r), int(c), int(sc), ctypes.byref(e)))
+        return e.iterations, e.smoothing
+
+    def grid(self, out=None):
+        """The grid as a (rows, cols) structured array {iterations, smoothing}."""
+        shape = (self.rows(), self.cols())
+        if out is None:
+            out = np.empty(shape, ESCAPE_DTYPE)
+        assert out.dtype == ESCAPE_DTYPE and out.shape == shape and out.flags.c_contiguous
+        _check(_lib.nm_get_grid(self._h, out.ctypes.data))
+        return out
+
+    def smoothing64(self):
+        out = np.empty((self.rows(), self.cols()), np.float64)
+        _check(_lib.nm_get_smoothing64(self._h, out.ctypes.data))
+        return out
+
+    def reduce(self, sc, out=None):
+        """scaleDown(sc)'s averaged grid, returned without changing the object."""
+        shape = (self.rows() // sc, self.cols() // sc)
+        if out is None:
+            out = np.empty(shape, ESCAPE_DTYPE)
+        assert out.dtype == ESCAPE_DTYPE and out.shape == shape and out.flags.c_contiguous
+        _check(_lib.nm_reduce(self._h, int(sc), out.ctypes.data))
+        return out
+
+    def device_grid(self):
+        g, s = ctypes.c_void_p(), ctypes.c_void_p()
+        _check(_lib.nm_device_grid(self._h, ctypes.byref(g), ctypes.byref(s)))
+        return g.value, s.value
+
+    def scaleUp(self, sc):
+        _check(_lib.nm_scale_up(self._h, int(sc)))
+
+    def scaleDown(self, sc):
+        _check(_lib.nm_scale_down(self._h, int(sc)))
+
+    # ---- view edits ------------------------------------------------------------
+    def pointAt(self, r, c, sc=1):
+        a = ctypes.create_string_buffer(1 << 16)
+        b = ctypes.create_string_buffer(1 << 16)
+        _check(_lib.nm_point_at(self._h, int(r), int(c), int(sc), a, b, len(a)))
+        return a.value.decode(), b.value.decode()
+
+    def translate(self, dr, dc, sc=1):
+        _check(_lib.nm_translate(self._h, int(dr), int(dc), int(sc)))
+
+    def zoom(self, scale):
+        _check(_lib.nm_zoom(self._h, float(scale)))
+
+    def zoomAt(self, scale, r, c, sc=1):
+        _check(_lib.nm_zoom_at(self._h, float(scale), int(r), int(c), int(sc)))
+
+    def loadLegacy(self, path):
+        _check(_lib.nm_load_legacy(self._h, _s(path)))
+
+    def save(self, path):
+        _check(_lib.nm_save(self._h, _s(path)))

@@ -1,0 +1,675 @@
+// The C ABI (include/newman_gb300.h): one nm_handle per reference
+// `Mandelbrot` object.  Host arbitrary-precision state in nmg::MPView, GPU
+// buffers and launches here.  There is no CPU path for per-sample work: if
+// the CUDA runtime or device is missing, every render call fails.
+#include "newman_gb300.h"
+
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "engine.hpp"
+#include "mpview.hpp"
+
+using nmg::Dbl2;
+using nmg::EscapeValue;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+#define NM_CUDA(call)                                                                  \
+  do {                                                                                 \
+    cudaError_t e_ = (call);                                                           \
+    if (e_ != cudaSuccess)                                                             \
+      return fail(NM_ERR_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
+                  __LINE__);                                                           \
+  } while (0)
+
+// Device buffer that grows on demand.
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  cudaError_t reserve(size_t count) {
+    if (count <= n && p) return cudaSuccess;
+    release();
+    cudaError_t e = cudaMalloc(&p, (count ? count : 1) * sizeof(T));
+    if (e == cudaSuccess) n = count;
+    return e;
+  }
+};
+
+static_assert(sizeof(nm_escape_value) == sizeof(EscapeValue), "grid layout");
+
+}  // namespace
+
+struct nm_handle {
+  nmg::MPView view;
+  int device = 0;
+  int path = NM_PATH_REFERENCE;
+  int tile_w = 16, tile_h = 16, chunk = 32, blocks = 0, threads = 0, renorm = 16;
+  bool keep_smooth64 = false;
+  cudaStream_t stream = nullptr;
+
+  // grid
+  DevBuf<EscapeValue> grid;
+  DevBuf<double> smooth64;
+  int grid_nr = 0, grid_nc = 0;
+
+  // per-view tables
+  std::vector<Dbl2> coord_re, coord_im;
+  std::vector<double> eps_re, eps_im;
+  nmg::OrbitData od;
+  bool precomputed = false;   // od + eps valid for the current view
+  bool coords_valid = false;  // coord tables valid for the current view
+  bool uploaded = false;      // device copies current
+  bool outside_cardioid = false;
+  double precompute_us = 0.0;
+  DevBuf<Dbl2> d_coord_re, d_coord_im, d_z, d_xhi, d_xlo, d_a, d_b, d_c;
+  DevBuf<double> d_eps_re, d_eps_im, d_sa_min;
+
+  // scratch: work counter + statistics
+  DevBuf<unsigned long long> d_scratch;
+  int* cancel_host = nullptr;
+  int* cancel_dev = nullptr;
+  long long expected_samples = 0;
+
+  nm_handle(int nr, int nc) : view(nr, nc) {}
+  ~nm_handle() {
+    if (stream) cudaStreamDestroy(stream);
+    if (cancel_host) cudaFreeHost(cancel_host);
+  }
+  void invalidate() {
+    precomputed = false;
+    coords_valid = false;
+    uploaded = false;
+  }
+};
+
+namespace {
+
+// The CUDA side of a handle is created on first use, so that the host-only
+// calls (view edits, the arbitrary-precision precompute) work without a GPU.
+int ensure_device(nm_handle* h) {
+  if (h->stream) return NM_OK;
+  NM_CUDA(cudaGetDevice(&h->device));
+  NM_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  NM_CUDA(cudaHostAlloc(&h->cancel_host, sizeof(int), cudaHostAllocMapped));
+  *h->cancel_host = 0;
+  NM_CUDA(cudaHostGetDevicePointer((void**)&h->cancel_dev, h->cancel_host, 0));
+  NM_CUDA(h->d_scratch.reserve(1 + nmg::STAT_COUNT));
+  NM_CUDA(cudaMemsetAsync(h->d_scratch.p, 0, (1 + nmg::STAT_COUNT) * 8, h->stream));
+  return NM_OK;
+}
+
+int ensure_grid(nm_handle* h) {
+  if (int rc = ensure_device(h)) return rc;
+  const int nr = h->view.rows(), nc = h->view.cols();
+  if (h->grid.p && h->grid_nr == nr && h->grid_nc == nc &&
+      (!h->keep_smooth64 || h->smooth64.p))
+    return NM_OK;
+  const size_t n = (size_t)nr * nc;
+  if (!(h->grid.p && h->grid_nr == nr && h->grid_nc == nc)) {
+    NM_CUDA(h->grid.reserve(n));
+    NM_CUDA(cudaMemsetAsync(h->grid.p, 0, n * sizeof(EscapeValue), h->stream));
+  }
+  if (h->keep_smooth64) {
+    NM_CUDA(h->smooth64.reserve(n));
+    NM_CUDA(cudaMemsetAsync(h->smooth64.p, 0, n * sizeof(double), h->stream));
+  }
+  h->grid_nr = nr;
+  h->grid_nc = nc;
+  return NM_OK;
+}
+
+template <typename T>
+int upload(DevBuf<T>& d, const std::vector<T>& v, cudaStream_t s) {
+  NM_CUDA(d.reserve(v.size()));
+  if (!v.empty())
+    NM_CUDA(cudaMemcpyAsync(d.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+  return NM_OK;
+}
+
+int ensure_coords(nm_handle* h) {
+  if (h->coords_valid) return NM_OK;
+  std::vector<nmg::D2> re, im;
+  h->view.coordinates(re, im);
+  h->coord_re.resize(re.size());
+  h->coord_im.resize(im.size());
+  for (size_t i = 0; i < re.size(); i++) h->coord_re[i] = {re[i].x, re[i].y};
+  for (size_t i = 0; i < im.size(); i++) h->coord_im[i] = {im[i].x, im[i].y};
+  h->outside_cardioid = h->view.view_outside_cardioid();
+  h->coords_valid = true;
+  h->uploaded = false;
+  return NM_OK;
+}
+
+int do_upload(nm_handle* h) {
+  int rc;
+  if ((rc = ensure_device(h))) return rc;
+  if ((rc = upload(h->d_coord_re, h->coord_re, h->stream))) return rc;
+  if ((rc = upload(h->d_coord_im, h->coord_im, h->stream))) return rc;
+  if (h->precomputed) {
+    auto cv = [](const std::vector<nmg::D2>& v) {
+      std::vector<Dbl2> o(v.size());
+      std::memcpy(o.data(), v.data(), v.size() * sizeof(Dbl2));
+      return o;
+    };
+    if ((rc = upload(h->d_eps_re, h->eps_re, h->stream))) return rc;
+    if ((rc = upload(h->d_eps_im, h->eps_im, h->stream))) return rc;
+    if ((rc = upload(h->d_z, cv(h->od.z), h->stream))) return rc;
+    if ((rc = upload(h->d_xhi, cv(h->od.xhi), h->stream))) return rc;
+    if ((rc = upload(h->d_xlo, cv(h->od.xlo), h->stream))) return rc;
+    if ((rc = upload(h->d_a, cv(h->od.a), h->stream))) return rc;
+    if ((rc = upload(h->d_b, cv(h->od.b), h->stream))) return rc;
+    if ((rc = upload(h->d_c, cv(h->od.c), h->stream))) return rc;
+    if ((rc = upload(h->d_sa_min, h->od.sa_min, h->stream))) return rc;
+  }
+  // The vectors above are pageable; the copies are complete when the stream
+  // reaches this point, so wait before the host may touch them again.
+  NM_CUDA(cudaStreamSynchronize(h->stream));
+  h->uploaded = true;
+  return NM_OK;
+}
+
+int check_handle(const nm_handle* h) {
+  if (!h) return fail(NM_ERR_ARG, "null handle");
+  return NM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* nm_last_error(void) { return g_last_error.c_str(); }
+
+nm_handle* nm_create(int nr, int nc) {
+  if (nr < 1 || nc < 1) {
+    fail(NM_ERR_ARG, "grid size %d x %d", nr, nc);
+    return nullptr;
+  }
+  return new nm_handle(nr, nc);
+}
+
+nm_handle* nm_copy(const nm_handle* src) {
+  if (!src) {
+    fail(NM_ERR_ARG, "null handle");
+    return nullptr;
+  }
+  std::unique_ptr<nm_handle> h(new nm_handle(1, 1));
+  h->view = src->view;
+  h->path = src->path;
+  h->tile_w = src->tile_w;
+  h->tile_h = src->tile_h;
+  h->chunk = src->chunk;
+  h->blocks = src->blocks;
+  h->threads = src->threads;
+  h->renorm = src->renorm;
+  h->keep_smooth64 = src->keep_smooth64;
+  h->coord_re = src->coord_re;
+  h->coord_im = src->coord_im;
+  h->eps_re = src->eps_re;
+  h->eps_im = src->eps_im;
+  h->od = src->od;
+  h->precomputed = src->precomputed;
+  h->coords_valid = src->coords_valid;
+  h->outside_cardioid = src->outside_cardioid;
+  if (!src->stream) return h.release();  // nothing on the GPU yet
+  if (ensure_grid(h.get()) != NM_OK) return nullptr;
+  cudaError_t e = cudaStreamSynchronize(src->stream);
+  const size_t n = (size_t)src->grid_nr * src->grid_nc;
+  if (e == cudaSuccess)
+    e = cudaMemcpy(h->grid.p, src->grid.p, n * sizeof(EscapeValue), cudaMemcpyDeviceToDevice);
+  if (e == cudaSuccess && src->keep_smooth64 && src->smooth64.p)
+    e = cudaMemcpy(h->smooth64.p, src->smooth64.p, n * sizeof(double), cudaMemcpyDeviceToDevice);
+  if (e != cudaSuccess) {
+    fail(NM_ERR_CUDA, "copy: %s", cudaGetErrorString(e));
+    return nullptr;
+  }
+  return h.release();
+}
+
+void nm_destroy(nm_handle* h) {
+  if (h) {
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    delete h;
+  }
+}
+
+int nm_set_view(nm_handle* h, const char* cre, const char* cim, const char* sre, const char* sim,
+                int N, double tol, int min_bits) {
+  if (int rc = check_handle(h)) return rc;
+  if (N < 1) return fail(NM_ERR_ARG, "N must be >= 1 (got %d)", N);
+  if (!(tol >= 0.0)) return fail(NM_ERR_ARG, "tolerance must be >= 0");
+  int rc = h->view.set_view(cre, cim, sre, sim, N, tol, min_bits);
+  if (rc == 1) return fail(NM_ERR_ARG, "null view string");
+  if (rc == 2) return fail(NM_ERR_PARSE, "view string does not parse as a decimal number");
+  h->invalidate();
+  return NM_OK;
+}
+
+int nm_get_view(const nm_handle* h, int which, char* buf, int buflen) {
+  if (int rc = check_handle(h)) return rc;
+  if (!buf || which < 0 || which > 3) return fail(NM_ERR_ARG, "bad view field %d", which);
+  std::string s = which == 0 ? h->view.center_re_str()
+                : which == 1 ? h->view.center_im_str()
+                : which == 2 ? h->view.step_re_str()
+                             : h->view.step_im_str();
+  if ((int)s.size() + 1 > buflen) return fail(NM_ERR_ARG, "buffer too small (%zu)", s.size() + 1);
+  std::memcpy(buf, s.c_str(), s.size() + 1);
+  return NM_OK;
+}
+
+int nm_set_iterations(nm_handle* h, int N) {
+  if (int rc = check_handle(h)) return rc;
+  if (N < 1) return fail(NM_ERR_ARG, "N must be >= 1 (got %d)", N);
+  h->view.set_iterations(N);
+  h->precomputed = false;
+  h->uploaded = false;
+  return NM_OK;
+}
+int nm_get_iterations(const nm_handle* h) { return h ? h->view.iterations() : -1; }
+int nm_set_tolerance(nm_handle* h, double tol) {
+  if (int rc = check_handle(h)) return rc;
+  if (!(tol >= 0.0)) return fail(NM_ERR_ARG, "tolerance must be >= 0");
+  h->view.set_tolerance(tol);
+  h->precomputed = false;
+  h->uploaded = false;
+  return NM_OK;
+}
+int nm_rows(const nm_handle* h) { return h ? h->view.rows() : -1; }
+int nm_cols(const nm_handle* h) { return h ? h->view.cols() : -1; }
+int nm_use_hardware(const nm_handle* h) { return h ? (h->view.use_hardware() ? 1 : 0) : -1; }
+
+int nm_set_path(nm_handle* h, int path) {
+  if (int rc = check_handle(h)) return rc;
+  if (path < NM_PATH_REFERENCE || path > NM_PATH_FE32) return fail(NM_ERR_ARG, "bad path %d", path);
+  h->path = path;
+  return NM_OK;
+}
+
+int nm_set_option(nm_handle* h, int opt, long long value) {
+  if (int rc = check_handle(h)) return rc;
+  switch (opt) {
+    case NM_OPT_TILE_W:
+    case NM_OPT_TILE_H:
+      if (value < 1 || value > 1024) return fail(NM_ERR_ARG, "tile size %lld", value);
+      (opt == NM_OPT_TILE_W ? h->tile_w : h->tile_h) = (int)value;
+      return NM_OK;
+    case NM_OPT_CHUNK:
+      if (value < 1 || value > (1 << 20)) return fail(NM_ERR_ARG, "chunk %lld", value);
+      h->chunk = (int)value;
+      return NM_OK;
+    case NM_OPT_KEEP_SMOOTH64:
+      h->keep_smooth64 = value != 0;
+      return h->stream ? ensure_grid(h) : NM_OK;
+    case NM_OPT_THREADS:
+      if (value < 0) return fail(NM_ERR_ARG, "threads %lld", value);
+      h->threads = (int)value;
+      return NM_OK;
+    case NM_OPT_BLOCKS:
+      if (value < 0 || value > (1 << 20)) return fail(NM_ERR_ARG, "blocks %lld", value);
+      h->blocks = (int)value;
+      return NM_OK;
+    case NM_OPT_RENORM:
+      if (value < 1 || value > 256) return fail(NM_ERR_ARG, "renorm interval %lld", value);
+      h->renorm = (int)value;
+      return NM_OK;
+  }
+  return fail(NM_ERR_ARG, "unknown option %d", opt);
+}
+
+int nm_get_stat(nm_handle* h, int stat, long long* value) {
+  if (int rc = check_handle(h)) return rc;
+  if (!value) return fail(NM_ERR_ARG, "null output");
+  if (stat >= 0 && stat < nmg::STAT_COUNT) {
+    unsigned long long v = 0;
+    if (!h->stream) {
+      *value = 0;
+      return NM_OK;
+    }
+    NM_CUDA(cudaStreamSynchronize(h->stream));
+    NM_CUDA(cudaMemcpy(&v, h->d_scratch.p + 1 + stat, 8, cudaMemcpyDeviceToHost));
+    *value = (long long)v;
+    return NM_OK;
+  }
+  switch (stat) {
+    case NM_STAT_ORBIT_LENGTH: *value = h->precomputed ? h->od.xlen : 0; return NM_OK;
+    case NM_STAT_PROBE_INDEX: *value = h->precomputed ? h->od.probe_index : -1; return NM_OK;
+    case NM_STAT_PRECISION_BITS: *value = (long long)h->view.bits(); return NM_OK;
+    case NM_STAT_PRECOMPUTE_US: *value = (long long)h->precompute_us; return NM_OK;
+  }
+  return fail(NM_ERR_ARG, "unknown stat %d", stat);
+}
+
+int nm_precompute(nm_handle* h) {
+  if (int rc = check_handle(h)) return rc;
+  auto t0 = std::chrono::steady_clock::now();
+  h->coords_valid = false;
+  if (int rc = ensure_coords(h)) return rc;
+  h->precomputed = false;
+  if (!h->view.use_hardware() || h->path != NM_PATH_REFERENCE) {
+    int threads = h->threads > 0 ? h->threads : (int)std::thread::hardware_concurrency();
+    if (h->view.precompute(threads, h->od)) return fail(NM_ERR_STATE, "precompute failed");
+    h->view.eps_tables(h->od, h->eps_re, h->eps_im);
+    h->precomputed = true;
+  }
+  h->precompute_us =
+      std::chrono::duration<double, std::micro>(std::chrono::steady_clock::now() - t0).count();
+  h->uploaded = false;  // copied to the GPU by nm_upload or the next render
+  return NM_OK;
+}
+
+int nm_upload(nm_handle* h) {
+  if (int rc = check_handle(h)) return rc;
+  if (int rc = ensure_coords(h)) return rc;
+  return do_upload(h);
+}
+
+int nm_render_rows(nm_handle* h, int r0, int r1, void* stream_arg) {
+  if (int rc = check_handle(h)) return rc;
+  const int nr = h->view.rows(), nc = h->view.cols();
+  if (r0 < 0 || r1 > nr || r0 > r1) return fail(NM_ERR_ARG, "rows [%d, %d) of %d", r0, r1, nr);
+  const bool hw = h->view.use_hardware() && h->path == NM_PATH_REFERENCE;
+  if (!hw && !h->precomputed)
+    return fail(NM_ERR_STATE, "deep view: nm_precompute must run before rendering");
+  if (int rc = ensure_grid(h)) return rc;
+  if (int rc = ensure_coords(h)) return rc;
+  if (!h->uploaded)
+    if (int rc = do_upload(h)) return rc;
+  cudaStream_t s = stream_arg ? (cudaStream_t)stream_arg : h->stream;
+
+  nmg::DeviceView v;
+  std::memset(&v, 0, sizeof v);
+  v.nr = nr;
+  v.nc = nc;
+  v.N = h->view.iterations();
+  v.cardioid_mode = h->outside_cardioid ? nmg::CARDIOID_NONE : nmg::CARDIOID_PER_SAMPLE;
+  v.tol = h->view.tolerance();
+  v.bailout2 = 1024.0 * 1024.0;
+  v.log_bailout = std::log(1024.0);
+  v.tile_w = h->tile_w;
+  v.tile_h = h->tile_h;
+  v.row0 = r0;
+  v.row1 = r1;
+  v.tiles_x = (nc + h->tile_w - 1) / h->tile_w;
+  v.tiles_y = (r1 - r0 + h->tile_h - 1) / h->tile_h;
+  v.total = (long long)v.tiles_x * v.tiles_y * h->tile_w * h->tile_h;
+  v.coord_re = h->d_coord_re.p;
+  v.coord_im = h->d_coord_im.p;
+  if (!hw) {
+    v.eps_re = h->d_eps_re.p;
+    v.eps_im = h->d_eps_im.p;
+    v.z = h->d_z.p;
+    v.zlen = (int)h->od.z.size();
+    v.xlen = h->od.xlen;
+    v.xhi = h->d_xhi.p;
+    v.xlo = h->d_xlo.p;
+    v.sa_a = h->d_a.p;
+    v.sa_b = h->d_b.p;
+    v.sa_c = h->d_c.p;
+    v.sa_min = h->d_sa_min.p;
+    v.sa_scan = h->od.sa_fp64_ok ? 0 : 1;
+  }
+  v.grid = h->grid.p;
+  v.smooth64 = h->keep_smooth64 ? h->smooth64.p : nullptr;
+
+  nmg::KernelKind kind = hw ? nmg::KERNEL_HW
+                       : (h->path == NM_PATH_FE32 ? nmg::KERNEL_FE32 : nmg::KERNEL_DELTA64);
+  nmg::RenderCtl ctl;
+  ctl.next = h->d_scratch.p;
+  ctl.stats = h->d_scratch.p + 1;
+  ctl.cancel = h->cancel_dev;
+  ctl.first = 0;
+  ctl.count = v.total;
+  *h->cancel_host = 0;
+  h->expected_samples = (long long)(r1 - r0) * nc;
+  NM_CUDA(cudaMemsetAsync(h->d_scratch.p, 0, (1 + nmg::STAT_COUNT) * 8, s));
+  if (v.total == 0) return NM_OK;
+  int blocks = h->blocks > 0 ? h->blocks : nmg::persistent_blocks(kind, h->device);
+  long long max_useful = (v.total + 31) / 32;  // one warp per 32 samples at most
+  long long warps_per_block = nmg::kernel_threads(kind) / 32;
+  long long need_blocks = (max_useful + warps_per_block - 1) / warps_per_block;
+  if (blocks > need_blocks) blocks = (int)need_blocks;
+  if (blocks < 1) blocks = 1;
+  int chunk = h->chunk;
+  if (kind == nmg::KERNEL_FE32) chunk = h->renorm;  // the FE32 kernel renormalises per chunk
+  NM_CUDA(nmg::launch_render(kind, v, ctl, s, blocks, chunk));
+  return NM_OK;
+}
+
+int nm_synchronize(nm_handle* h) {
+  if (int rc = check_handle(h)) return rc;
+  if (!h->stream) return NM_OK;
+  NM_CUDA(cudaStreamSynchronize(h->stream));
+  if (*h->cancel_host) {
+    unsigned long long done = 0;
+    NM_CUDA(cudaMemcpy(&done, h->d_scratch.p + 1 + nmg::STAT_SAMPLES, 8, cudaMemcpyDeviceToHost));
+    if ((long long)done < h->expected_samples)
+      return fail(NM_ERR_CANCELLED, "render cancelled after %llu of %lld samples", done,
+                  h->expected_samples);
+  }
+  return NM_OK;
+}
+
+int nm_render(nm_handle* h) {
+  if (int rc = nm_render_rows(h, 0, h ? h->view.rows() : 0, nullptr)) return rc;
+  return nm_synchronize(h);
+}
+
+int nm_compute_row(nm_handle* h, int r) {
+  if (int rc = nm_render_rows(h, r, r + 1, nullptr)) return rc;
+  return nm_synchronize(h);
+}
+
+int nm_cancel(nm_handle* h) {
+  if (int rc = check_handle(h)) return rc;
+  *(volatile int*)h->cancel_host = 1;
+  return NM_OK;
+}
+
+int nm_at(nm_handle* h, int r, int c, nm_escape_value* out) {
+  if (int rc = check_handle(h)) return rc;
+  if (int rc = ensure_grid(h)) return rc;
+  if (!out || r < 0 || c < 0 || r >= h->grid_nr || c >= h->grid_nc)
+    return fail(NM_ERR_ARG, "at(%d, %d) outside %d x %d", r, c, h->grid_nr, h->grid_nc);
+  NM_CUDA(cudaStreamSynchronize(h->stream));
+  NM_CUDA(cudaMemcpy(out, h->grid.p + (size_t)r * h->grid_nc + c, sizeof(EscapeValue),
+                     cudaMemcpyDeviceToHost));
+  return NM_OK;
+}
+
+int nm_at_sc(nm_handle* h, int r, int c, int sc, nm_escape_value* out) {
+  if (int rc = check_handle(h)) return rc;
+  if (int rc = ensure_grid(h)) return rc;
+  if (!out || sc < 1 || r < 0 || c < 0 || (long long)sc * (r + 1) > h->grid_nr ||
+      (long long)sc * (c + 1) > h->grid_nc)
+    return fail(NM_ERR_ARG, "at(%d, %d, %d) outside %d x %d", r, c, sc, h->grid_nr, h->grid_nc);
+  NM_CUDA(cudaStreamSynchronize(h->stream));
+  std::vector<EscapeValue> block((size_t)sc * sc);
+  for (int r1 = 0; r1 < sc; r1++)
+    NM_CUDA(cudaMemcpy(block.data() + (size_t)r1 * sc,
+                       h->grid.p + (size_t)(sc * r + r1) * h->grid_nc + (size_t)sc * c,
+                       sc * sizeof(EscapeValue), cudaMemcpyDeviceToHost));
+  // mandelbrot.cpp:322-330
+  float sum = 0.0f;
+  for (const EscapeValue& e : block) sum += e.iterations + e.smoothing;
+  sum /= sc * sc;
+  out->iterations = (int)sum;
+  out->smoothing = sum - out->iterations;
+  return NM_OK;
+}
+
+int nm_reduce(nm_handle* h, int sc, nm_escape_value* host_out) {
+  if (int rc = check_handle(h)) return rc;
+  if (int rc = ensure_grid(h)) return rc;
+  if (!host_out || sc < 1) return fail(NM_ERR_ARG, "bad reduce arguments");
+  const int nr = h->grid_nr / sc, nc = h->grid_nc / sc;
+  DevBuf<EscapeValue> tmp;
+  NM_CUDA(tmp.reserve((size_t)nr * nc));
+  NM_CUDA(nmg::launch_reduce(h->grid.p, nr, nc, sc, tmp.p, h->stream));
+  NM_CUDA(cudaMemcpyAsync(host_out, tmp.p, (size_t)nr * nc * sizeof(EscapeValue),
+                          cudaMemcpyDeviceToHost, h->stream));
+  NM_CUDA(cudaStreamSynchronize(h->stream));
+  return NM_OK;
+}
+
+int nm_scale_up(nm_handle* h, int sc) {
+  if (int rc = check_handle(h)) return rc;
+  if (sc < 1) return fail(NM_ERR_ARG, "scale %d", sc);
+  if (!h->stream) {  // no grid on the GPU yet: all zeros, nothing to duplicate
+    h->view.scale_up(sc);
+    h->invalidate();
+    return NM_OK;
+  }
+  if (int rc = ensure_grid(h)) return rc;
+  const int nr = h->grid_nr, nc = h->grid_nc;
+  DevBuf<EscapeValue> bigger;
+  NM_CUDA(bigger.reserve((size_t)nr * sc * nc * sc));
+  NM_CUDA(nmg::launch_duplicate(h->grid.p, nr, nc, sc, bigger.p, h->stream));
+  NM_CUDA(cudaStreamSynchronize(h->stream));
+  std::swap(h->grid.p, bigger.p);
+  std::swap(h->grid.n, bigger.n);
+  h->grid_nr = nr * sc;
+  h->grid_nc = nc * sc;
+  h->smooth64.release();
+  h->view.scale_up(sc);
+  h->invalidate();
+  return ensure_grid(h);
+}
+
+int nm_scale_down(nm_handle* h, int sc) {
+  if (int rc = check_handle(h)) return rc;
+  if (sc < 1) return fail(NM_ERR_ARG, "scale %d", sc);
+  if (!h->stream) {  // no grid on the GPU yet: the mean of zeros is zero
+    h->view.scale_down(sc);
+    h->invalidate();
+    return NM_OK;
+  }
+  if (int rc = ensure_grid(h)) return rc;
+  const int nr = h->grid_nr / sc, nc = h->grid_nc / sc;
+  DevBuf<EscapeValue> smaller;
+  NM_CUDA(smaller.reserve((size_t)nr * nc));
+  NM_CUDA(nmg::launch_reduce(h->grid.p, nr, nc, sc, smaller.p, h->stream));
+  NM_CUDA(cudaStreamSynchronize(h->stream));
+  std::swap(h->grid.p, smaller.p);
+  std::swap(h->grid.n, smaller.n);
+  h->grid_nr = nr;
+  h->grid_nc = nc;
+  h->smooth64.release();
+  h->view.scale_down(sc);
+  h->invalidate();
+  return ensure_grid(h);
+}
+
+int nm_get_grid(nm_handle* h, nm_escape_value* host_out) {
+  if (int rc = check_handle(h)) return rc;
+  if (int rc = ensure_grid(h)) return rc;
+  if (!host_out) return fail(NM_ERR_ARG, "null output");
+  NM_CUDA(cudaMemcpyAsync(host_out, h->grid.p, (size_t)h->grid_nr * h->grid_nc * 8,
+                          cudaMemcpyDeviceToHost, h->stream));
+  NM_CUDA(cudaStreamSynchronize(h->stream));
+  return NM_OK;
+}
+
+int nm_get_smoothing64(nm_handle* h, double* host_out) {
+  if (int rc = check_handle(h)) return rc;
+  if (int rc = ensure_grid(h)) return rc;
+  if (!host_out) return fail(NM_ERR_ARG, "null output");
+  if (!h->keep_smooth64 || !h->smooth64.p)
+    return fail(NM_ERR_STATE, "NM_OPT_KEEP_SMOOTH64 is off");
+  NM_CUDA(cudaMemcpyAsync(host_out, h->smooth64.p, (size_t)h->grid_nr * h->grid_nc * 8,
+                          cudaMemcpyDeviceToHost, h->stream));
+  NM_CUDA(cudaStreamSynchronize(h->stream));
+  return NM_OK;
+}
+
+int nm_device_grid(nm_handle* h, nm_escape_value** grid, double** smooth64) {
+  if (int rc = check_handle(h)) return rc;
+  if (int rc = ensure_grid(h)) return rc;
+  if (grid) *grid = reinterpret_cast<nm_escape_value*>(h->grid.p);
+  if (smooth64) *smooth64 = h->keep_smooth64 ? h->smooth64.p : nullptr;
+  return NM_OK;
+}
+
+int nm_point_at(const nm_handle* h, int r, int c, int sc, char* re, char* im, int buflen) {
+  if (int rc = check_handle(h)) return rc;
+  if (!re || !im) return fail(NM_ERR_ARG, "null output");
+  nmg::Mpf pr(64), pi(64);
+  h->view.point_at(r, c, sc, pr, pi);
+  std::string a = nmg::MPView::to_string(pr), b = nmg::MPView::to_string(pi);
+  if ((int)std::max(a.size(), b.size()) + 1 > buflen) return fail(NM_ERR_ARG, "buffer too small");
+  std::memcpy(re, a.c_str(), a.size() + 1);
+  std::memcpy(im, b.c_str(), b.size() + 1);
+  return NM_OK;
+}
+
+int nm_translate(nm_handle* h, int dr, int dc, int sc) {
+  if (int rc = check_handle(h)) return rc;
+  h->view.translate(dr, dc, sc);
+  h->invalidate();
+  return NM_OK;
+}
+
+int nm_zoom(nm_handle* h, float scale) {
+  if (int rc = check_handle(h)) return rc;
+  if (!(scale > 0.0f)) return fail(NM_ERR_ARG, "zoom scale must be > 0");
+  h->view.zoom(scale);
+  h->invalidate();
+  return NM_OK;
+}
+
+int nm_zoom_at(nm_handle* h, float scale, int r, int c, int sc) {
+  if (int rc = check_handle(h)) return rc;
+  if (!(scale > 0.0f)) return fail(NM_ERR_ARG, "zoom scale must be > 0");
+  h->view.zoom_at(scale, r, c, sc);
+  h->invalidate();
+  return NM_OK;
+}
+
+int nm_load_legacy(nm_handle* h, const char* path) {
+  if (int rc = check_handle(h)) return rc;
+  if (!path) return fail(NM_ERR_ARG, "null path");
+  int rc = h->view.load_legacy(path);
+  if (rc == 1) return fail(NM_ERR_IO, "cannot open %s", path);
+  if (rc == 2) return fail(NM_ERR_PARSE, "malformed view file %s", path);
+  h->invalidate();
+  return NM_OK;
+}
+
+int nm_save(const nm_handle* h, const char* path) {
+  if (int rc = check_handle(h)) return rc;
+  if (!path) return fail(NM_ERR_ARG, "null path");
+  if (h->view.save(path)) return fail(NM_ERR_IO, "cannot write %s", path);
+  return NM_OK;
+}
+
+}  // extern "C"

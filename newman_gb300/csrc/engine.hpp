@@ -1,0 +1,45 @@
+// Launch interface of the per-sample kernels (host side, C++).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "view_device.cuh"
+
+namespace nmg {
+
+enum StatIndex {
+  STAT_CARDIOID_UNDECIDED = 0,  // double-double cardioid test within 2^-96 of zero
+  STAT_EXECUTED_ITERS = 1,      // z -> z^2 + c steps run on the GPU
+  STAT_SAMPLES = 2,             // samples finished
+  STAT_REBASES = 3,             // rebases of the perturbation delta
+  STAT_GLITCHES = 4,            // FP32 steps redone in FP64 near a threshold
+  STAT_COUNT = 8
+};
+
+// Work distribution and bookkeeping of one persistent launch.  `next` and
+// `stats` live in device scratch memory that the caller zeroes.
+struct RenderCtl {
+  unsigned long long* next;      // work counter, samples handed out so far
+  unsigned long long* stats;     // [STAT_COUNT]
+  const volatile int* cancel;    // host-mapped flag, may be null
+  long long first;               // first sample index (tile order)
+  long long count;               // samples in this launch
+};
+
+enum KernelKind { KERNEL_HW = 0, KERNEL_DELTA64 = 1, KERNEL_FE32 = 2 };
+
+// Persistent, warp-refilled launches: every warp keeps its 32 lanes busy by
+// pulling new samples from `ctl.next` as lanes finish.
+cudaError_t launch_render(KernelKind kind, const DeviceView& v, const RenderCtl& ctl,
+                          cudaStream_t stream, int blocks, int chunk);
+int persistent_blocks(KernelKind kind, int device);
+int kernel_threads(KernelKind kind);
+
+// Multisample mean (mandelbrot.cpp:320-332): (nr*sc x nc*sc) -> (nr x nc).
+cudaError_t launch_reduce(const EscapeValue* in, int nr, int nc, int sc, EscapeValue* out,
+                          cudaStream_t stream);
+// Value duplication of scaleUp (mandelbrot.cpp:334-341): (nr x nc) -> (nr*sc x nc*sc).
+cudaError_t launch_duplicate(const EscapeValue* in, int nr, int nc, int sc, EscapeValue* out,
+                             cudaStream_t stream);
+
+}  // namespace nmg

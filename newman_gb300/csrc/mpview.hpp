@@ -1,0 +1,120 @@
+// Host-side arbitrary-precision view state of one render: the center, the
+// pixel step, the iteration count and the precision rule of the reference's
+// `Mandelbrot` object (mandelbrot.h:7-53), plus the sequential precompute
+// (probe search, reference orbit, series coefficients) that feeds the GPU.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "gmp_abi.h"
+
+namespace nmg {
+
+// One mpf_t with value semantics (copying keeps the precision).
+class Mpf {
+ public:
+  explicit Mpf(unsigned long bits = 64) { mpf_init2(v_, bits); }
+  Mpf(const Mpf& o) {
+    mpf_init2(v_, mpf_get_prec(o.v_));
+    mpf_set(v_, o.v_);
+  }
+  Mpf& operator=(const Mpf& o) {
+    if (this != &o) {
+      mpf_set_prec(v_, mpf_get_prec(o.v_));
+      mpf_set(v_, o.v_);
+    }
+    return *this;
+  }
+  ~Mpf() { mpf_clear(v_); }
+  void swap(Mpf& o) {  // exchanges the limb buffers, no copy
+    __mpf_struct t = v_[0];
+    v_[0] = o.v_[0];
+    o.v_[0] = t;
+  }
+  mpf_ptr p() { return v_; }
+  mpf_srcptr p() const { return v_; }
+  double d() const { return mpf_get_d(v_); }
+
+ private:
+  mpf_t v_;
+};
+
+struct D2 {
+  double x, y;
+};
+
+// What one precompute hands to the device, all as FP64 values read from the
+// arbitrary-precision state with get_d (truncation toward zero, like
+// complex.h:33-35 `descend`).
+struct OrbitData {
+  int xlen = 0;                 // X.size() of the reference after findProbe
+  int probe_index = -1;         // which probe won (mandelbrot.cpp:85-94)
+  std::vector<D2> z;            // 0, X[0..xlen), and the escaped element if any
+  std::vector<D2> xhi, xlo;     // X[k] = xhi + xlo (+ < 2^-106 |X|)
+  std::vector<D2> a, b, c;      // series coefficients A, B, C
+  std::vector<double> sa_min;   // prefix minimum of tol |B_i|^2 / |C_i|^2 (index 0 unused)
+  bool sa_fp64_ok = true;       // FP64 series terms stay in the normal range
+};
+
+class MPView {
+ public:
+  MPView(int nr, int nc);
+
+  int rows() const { return nr_; }
+  int cols() const { return nc_; }
+  int iterations() const { return N_; }
+  double tolerance() const { return tol_; }
+  unsigned long bits() const { return bits_; }
+
+  // center / step as decimal strings, N, series tolerance, precision floor.
+  int set_view(const char* cre, const char* cim, const char* sre, const char* sim, int N,
+               double tol, int min_bits);
+  void set_iterations(int N);
+  void set_tolerance(double tol) { tol_ = tol; }
+
+  bool use_hardware() const;  // mandelbrot.cpp:256-259
+  void scale_up(int sc);      // mandelbrot.cpp:334-346 (geometry)
+  void scale_down(int sc);    // mandelbrot.cpp:348-360 (geometry)
+  void zoom(float scale);     // mandelbrot.cpp:297-302
+  void zoom_at(float scale, int r, int c, int sc);  // mandelbrot.cpp:304-316
+  void translate(int dr, int dc, int sc);           // mandelbrot.cpp:292-295
+  void point_at(int r, int c, int sc, Mpf& re, Mpf& im) const;  // mandelbrot.cpp:285-290
+  int load_legacy(const char* path);                // mandelbrot.cpp:19-35
+  int save(const char* path) const;                 // viewer.cpp:12-23 format
+
+  std::string center_re_str() const { return to_string(cre_); }
+  std::string center_im_str() const { return to_string(cim_); }
+  std::string step_re_str() const { return to_string(sre_); }
+  std::string step_im_str() const { return to_string(sim_); }
+  static std::string to_string(const Mpf& f);
+
+  // Per-column real and per-row imaginary sample coordinates (computeRow's
+  // pt.re / pt.im, mandelbrot.cpp:271,275), as hi + lo doubles.
+  void coordinates(std::vector<D2>& re, std::vector<D2>& im) const;
+  // eps = get_d(pt - X[0]) per column / row (mandelbrot.cpp:155-159).
+  void eps_tables(const OrbitData& od, std::vector<double>& er, std::vector<double>& ei) const;
+
+  // findProbe + computeSeries (mandelbrot.cpp:73-131), probes on `threads`
+  // host threads.  Fills `out`.
+  int precompute(int threads, OrbitData& out);
+
+  // Box in which every sample lies is provably outside both the main
+  // cardioid and the period-2 disk.
+  bool view_outside_cardioid() const;
+
+ private:
+  void set_precision();  // mandelbrot.cpp:37-56
+  void coord_re(int c, Mpf& out, Mpf& tmp) const;
+  void coord_im(int r, Mpf& out, Mpf& tmp) const;
+
+  int nr_, nc_;
+  int N_ = 256;
+  double tol_ = 1e-10;
+  unsigned long bits_ = 64, min_bits_ = 0;
+  Mpf cre_, cim_, sre_, sim_;
+  Mpf x0re_, x0im_;  // X[0] of the last precompute
+};
+
+}  // namespace nmg

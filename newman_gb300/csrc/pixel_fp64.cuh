@@ -1,0 +1,351 @@
+// Per-sample FP64 arithmetic of the reference's per-pixel path.
+//
+// Every multiply and add of the reference's `double` code is written with a
+// round-to-nearest intrinsic (never contracted into an FMA), in the grouping
+// of complex.h:19-31 and mandelbrot.cpp, so that the results are the
+// reference's bit for bit.  FMAs appear only inside the double-double helpers
+// used for the cardioid test and the truncating sum X[k] + d.
+#pragma once
+
+#include <cmath>
+
+#include "view_device.cuh"
+
+namespace nmg {
+
+#if defined(__CUDA_ARCH__)
+NM_HD double mul_(double a, double b) { return __dmul_rn(a, b); }
+NM_HD double add_(double a, double b) { return __dadd_rn(a, b); }
+NM_HD double sub_(double a, double b) { return __dsub_rn(a, b); }
+NM_HD double fma_(double a, double b, double c) { return __fma_rn(a, b, c); }
+NM_HD double add_rz_(double a, double b) { return __dadd_rz(a, b); }
+NM_HD double log_(double x) { return log(x); }
+NM_HD double log2_(double x) { return log2(x); }
+#else
+inline double mul_(double a, double b) { return a * b; }
+inline double add_(double a, double b) { return a + b; }
+inline double sub_(double a, double b) { return a - b; }
+inline double fma_(double a, double b, double c) { return std::fma(a, b, c); }
+inline double add_rz_(double a, double b) {
+  double s = a + b;
+  double bb = s - a;
+  double err = (a - (s - bb)) + (b - bb);
+  if (err != 0.0 && ((err < 0.0) != (s < 0.0))) s = std::nextafter(s, 0.0);
+  return s;
+}
+inline double log_(double x) { return std::log(x); }
+inline double log2_(double x) { return std::log2(x); }
+#endif
+
+// ---- complex.h in the reference's order -----------------------------------
+struct C64 {
+  double re, im;
+};
+NM_HD C64 c_sq(C64 a) {  // complex.h:19-21
+  return {sub_(mul_(a.re, a.re), mul_(a.im, a.im)), mul_(mul_(2.0, a.re), a.im)};
+}
+NM_HD C64 c_add(C64 a, C64 b) { return {add_(a.re, b.re), add_(a.im, b.im)}; }
+NM_HD C64 c_mul(C64 a, C64 b) {  // complex.h:29-31
+  return {sub_(mul_(a.re, b.re), mul_(a.im, b.im)), add_(mul_(a.re, b.im), mul_(a.im, b.re))};
+}
+NM_HD double c_mag2(C64 a) { return add_(mul_(a.re, a.re), mul_(a.im, a.im)); }
+
+// mandelbrot.cpp:133-136
+NM_HD double smoothing_of(double r2, double log_bailout) {
+  return 1.0 - log2_(0.5 * log_(r2) / log_bailout);
+}
+
+// ---- double-double helpers -------------------------------------------------
+struct DD {
+  double hi, lo;
+};
+NM_HD DD two_sum(double a, double b) {
+  double s = add_(a, b);
+  double bb = sub_(s, a);
+  double err = add_(sub_(a, sub_(s, bb)), sub_(b, bb));
+  return {s, err};
+}
+NM_HD DD quick_two_sum(double a, double b) {
+  double s = add_(a, b);
+  return {s, sub_(b, sub_(s, a))};
+}
+NM_HD DD dd_add(DD a, DD b) {
+  DD s = two_sum(a.hi, b.hi);
+  DD t = two_sum(a.lo, b.lo);
+  s.lo = add_(s.lo, t.hi);
+  s = quick_two_sum(s.hi, s.lo);
+  s.lo = add_(s.lo, t.lo);
+  return quick_two_sum(s.hi, s.lo);
+}
+NM_HD DD dd_mul(DD a, DD b) {
+  double p = mul_(a.hi, b.hi);
+  double e = fma_(a.hi, b.hi, -p);
+  e = add_(e, add_(mul_(a.hi, b.lo), mul_(a.lo, b.hi)));
+  return quick_two_sum(p, e);
+}
+NM_HD double dd_abs_hi(DD a) { return a.hi < 0 ? -a.hi : a.hi; }
+
+// mandelbrot.cpp:63-71 on the sample's coordinates held as hi + lo (106
+// bits).  The reference evaluates in >= 128-bit mpf; the two can disagree
+// only when a polynomial lies within ~2^-100 of zero, which `undecided`
+// reports.
+NM_HD bool in_cardioid_dd(Dbl2 px, Dbl2 py, bool& undecided) {
+  const DD x{px.x, px.y}, y{py.x, py.y};
+  const DD fourth{0.25, 0.0};
+  DD xmf = dd_add(x, DD{-0.25, 0.0});
+  DD y2 = dd_mul(y, y);
+  DD q = dd_add(dd_mul(xmf, xmf), y2);
+  DD lhs = dd_mul(q, dd_add(q, xmf));
+  DD rhs = dd_mul(fourth, y2);
+  DD g = dd_add(lhs, DD{-rhs.hi, -rhs.lo});
+  const double tiny = 0x1p-96;
+  double bound = tiny * (dd_abs_hi(lhs) + dd_abs_hi(rhs)) + 1e-300;
+  undecided = false;
+  if (dd_abs_hi(g) <= bound) undecided = true;
+  if (g.hi < 0.0) return true;
+  DD q2 = dd_add(x, DD{1.0, 0.0});
+  DD lhs2 = dd_add(dd_mul(q2, q2), y2);
+  DD g2 = dd_add(lhs2, DD{-0.0625, 0.0});
+  if (dd_abs_hi(g2) <= tiny * (dd_abs_hi(lhs2) + 0.0625)) undecided = true;
+  return g2.hi < 0.0;
+}
+
+// get_d(X[k] + d): the arbitrary-precision sum of mandelbrot.cpp:184-185,
+// truncated toward zero like mpf_get_d, from X[k] = hi + lo.
+NM_HD double trunc_sum(double hi, double lo, double d) {
+  DD s = two_sum(hi, d);
+  return add_rz_(s.hi, add_(s.lo, lo));
+}
+
+// ---- the reference's double path (mandelbrot.cpp:231-254) ------------------
+struct HwState {
+  double z0r, z0i, zr, zi;
+  int32_t it;
+};
+
+// Returns true when the sample is already decided (cardioid).
+NM_HD bool hw_init(const DeviceView& v, int r, int c, HwState& st, EscapeValue& out, double& sm,
+                   bool& undecided) {
+  const Dbl2 px = v.coord_re[c], py = v.coord_im[r];
+  undecided = false;
+  if (v.cardioid_mode == CARDIOID_PER_SAMPLE && in_cardioid_dd(px, py, undecided)) {
+    out = {v.N, 0.0f};
+    sm = 0.0;
+    return true;
+  }
+  st.z0r = px.x;
+  st.z0i = py.x;
+  st.zr = px.x;
+  st.zi = py.x;
+  st.it = 0;
+  return false;
+}
+
+// Up to `steps` iterations of Z = sq(Z) + Z0; true when the sample is done.
+NM_HD bool hw_steps(const DeviceView& v, HwState& st, int steps, EscapeValue& out, double& sm) {
+  double zr = st.zr, zi = st.zi;
+  int it = st.it;
+  const int stop = (v.N - it < steps) ? v.N : it + steps;
+  for (; it < stop; it++) {
+    double nre = add_(sub_(mul_(zr, zr), mul_(zi, zi)), st.z0r);
+    double nim = add_(mul_(mul_(2.0, zr), zi), st.z0i);
+    zr = nre;
+    zi = nim;
+    double r2 = add_(mul_(zr, zr), mul_(zi, zi));
+    if (r2 > v.bailout2) {
+      sm = smoothing_of(r2, v.log_bailout);
+      out = {it, (float)sm};
+      return true;
+    }
+  }
+  st.zr = zr;
+  st.zi = zi;
+  st.it = it;
+  if (it >= v.N) {
+    out = {v.N, 0.0f};
+    sm = 0.0;
+    return true;
+  }
+  return false;
+}
+
+// ---- the series front of getIterations (mandelbrot.cpp:144-207) -------------
+struct SeriesFront {
+  C64 eps;       // Y0 - X[0]
+  C64 dfound;    // d[found]
+  int32_t dsize; // d.size() after the skip
+};
+
+NM_HD C64 sa_term(const DeviceView& v, int i, C64 eps, C64 eps2, C64 eps3, bool& unstable) {
+  const Dbl2 A = v.sa_a[i], B = v.sa_b[i], Cc = v.sa_c[i];
+  C64 a = c_mul(C64{A.x, A.y}, eps);
+  C64 b = c_mul(C64{B.x, B.y}, eps2);
+  C64 c = c_mul(C64{Cc.x, Cc.y}, eps3);
+  double bmag = add_(mul_(b.re, b.re), mul_(b.im, b.im));
+  double cmag = add_(mul_(c.re, c.re), mul_(c.im, c.im));
+  unstable = mul_(bmag, v.tol) < cmag;  // mandelbrot.cpp:138-142
+  return c_add(c_add(a, b), c);
+}
+
+NM_HD C64 sa_value(const DeviceView& v, int i, C64 eps, C64 eps2, C64 eps3) {
+  if (i == 0) return eps;
+  bool u;
+  return sa_term(v, i, eps, eps2, eps3, u);
+}
+
+// First index i in [lo, hi) with sa_min[i] < t (sa_min is non-increasing), or hi.
+NM_HD int first_below(const double* m, int lo, int hi, double t) {
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (m[mid] < t)
+      hi = mid;
+    else
+      lo = mid + 1;
+  }
+  return lo;
+}
+
+// The index at which the reference's loop (mandelbrot.cpp:165-181) first sees
+// an unstable term, or xlen when none.  The test tol|B_i eps2|^2 < |C_i eps3|^2
+// is, in exact arithmetic, T_i < u with T_i = tol|B_i|^2/|C_i|^2 and
+// u = |eps3|^2/|eps2|^2; the FP64 evaluation differs from exact by far less
+// than 2^-40 relative.  So the prefix minimum of T_i locates the first firing
+// term by binary search, and only terms whose ratio lies within 2^-40 of 1
+// are re-evaluated exactly as the reference does.
+NM_HD int sa_first_unstable(const DeviceView& v, C64 eps, C64 eps2, C64 eps3) {
+  const int n = v.xlen;
+  if (v.sa_scan) {
+    for (int i = 1; i < n; i++) {
+      bool u;
+      sa_term(v, i, eps, eps2, eps3, u);
+      if (u) return i;
+    }
+    return n;
+  }
+  const double m2 = c_mag2(eps2), m3 = c_mag2(eps3);
+  if (!(m2 > 0.0) || !(m3 > 0.0)) return n;  // b = c = 0 or c = 0: never unstable
+  const double u = m3 / m2;
+  const double hi_u = u * (1.0 + 0x1p-40), lo_u = u * (1.0 - 0x1p-40);
+  const int i_fp = first_below(v.sa_min, 1, n, hi_u);
+  if (i_fp >= n) return n;
+  const int i_c = first_below(v.sa_min, i_fp, n, lo_u);
+  for (int i = i_fp; i < i_c; i++) {
+    bool un;
+    sa_term(v, i, eps, eps2, eps3, un);
+    if (un) return i;
+  }
+  return i_c;  // fires for certain, or n
+}
+
+// Returns true when the sample is finished in the front half (cardioid, or
+// escaped before the skip point -- the binary search of :186-207).
+NM_HD bool series_front(const DeviceView& v, int r, int c, SeriesFront& f, EscapeValue& out,
+                        double& sm, bool& undecided) {
+  undecided = false;
+  if (v.cardioid_mode == CARDIOID_PER_SAMPLE &&
+      in_cardioid_dd(v.coord_re[c], v.coord_im[r], undecided)) {
+    out = {v.N, 0.0f};
+    sm = 0.0;
+    return true;
+  }
+  const C64 eps{v.eps_re[c], v.eps_im[r]};
+  const C64 eps2 = c_sq(eps);
+  const C64 eps3 = c_mul(eps, eps2);
+  const int fire = sa_first_unstable(v, eps, eps2, eps3);
+  int dsize = v.xlen;
+  if (fire < v.xlen) dsize = fire - 3 < 1 ? 1 : fire - 3;
+  int found = dsize - 1;
+  C64 d = sa_value(v, found, eps, eps2, eps3);
+  double yr = trunc_sum(v.xhi[found].x, v.xlo[found].x, d.re);
+  double yi = trunc_sum(v.xhi[found].y, v.xlo[found].y, d.im);
+  double r2 = add_(mul_(yr, yr), mul_(yi, yi));
+  if (r2 > v.bailout2) {
+    int low = 0, high = dsize - 1, mid = dsize / 2;
+    while (low <= high) {
+      C64 dm = sa_value(v, mid, eps, eps2, eps3);
+      double mr = trunc_sum(v.xhi[mid].x, v.xlo[mid].x, dm.re);
+      double mi = trunc_sum(v.xhi[mid].y, v.xlo[mid].y, dm.im);
+      if (!(add_(mul_(mr, mr), mul_(mi, mi)) > v.bailout2))
+        low = mid + 1;
+      else {
+        high = mid - 1;
+        found = mid;
+      }
+      mid = (low + high) / 2;
+    }
+    d = sa_value(v, found, eps, eps2, eps3);
+    yr = trunc_sum(v.xhi[found].x, v.xlo[found].x, d.re);
+    yi = trunc_sum(v.xhi[found].y, v.xlo[found].y, d.im);
+    sm = smoothing_of(add_(mul_(yr, yr), mul_(yi, yi)), v.log_bailout);
+    out = {found, (float)sm};
+    return true;
+  }
+  f.eps = eps;
+  f.dfound = d;
+  f.dsize = dsize;
+  return false;
+}
+
+// ---- plain FP64 perturbation continuation ---------------------------------
+// The pixel is Y = Z[j] + delta against the FP64 reference orbit Z (Z[0] = 0,
+// Z[k+1] = X[k]); one step is
+//     t = 2 Z[j] + delta;  delta = t * delta + eps;  j += 1;  Y = Z[j] + delta
+// and the pixel rebases to Z[0] (delta = Y, j = 0) when |Y| < |delta| or the
+// orbit is exhausted.  `i` counts like getIterations' continuation (:212).
+struct DeltaState {
+  double dr, di, er, ei;
+  int32_t j, i;
+};
+
+NM_HD void delta_start(const SeriesFront& f, DeltaState& st) {
+  st.dr = f.dfound.re;
+  st.di = f.dfound.im;
+  st.er = f.eps.re;
+  st.ei = f.eps.im;
+  st.j = f.dsize;  // found + 1
+  st.i = f.dsize;
+}
+
+NM_HD bool delta_steps(const DeviceView& v, DeltaState& st, int steps, EscapeValue& out,
+                       double& sm) {
+  double dr = st.dr, di = st.di;
+  int j = st.j, i = st.i;
+  const int zlast = v.zlen - 1;
+  const int stop = (v.N - i < steps) ? v.N : i + steps;
+  for (; i < stop; i++) {
+    const Dbl2 z = v.z[j];
+    double tr = add_(mul_(2.0, z.x), dr);
+    double ti = add_(mul_(2.0, z.y), di);
+    double nre = add_(sub_(mul_(tr, dr), mul_(ti, di)), st.er);
+    double nim = add_(add_(mul_(tr, di), mul_(ti, dr)), st.ei);
+    dr = nre;
+    di = nim;
+    j++;
+    const Dbl2 zn = v.z[j];
+    double yr = add_(zn.x, dr), yi = add_(zn.y, di);
+    double r2 = add_(mul_(yr, yr), mul_(yi, yi));
+    if (r2 > v.bailout2) {
+      sm = smoothing_of(r2, v.log_bailout);
+      out = {i, (float)sm};
+      return true;
+    }
+    double d2 = add_(mul_(dr, dr), mul_(di, di));
+    if (r2 < d2 || j == zlast) {
+      dr = yr;
+      di = yi;
+      j = 0;
+    }
+  }
+  st.dr = dr;
+  st.di = di;
+  st.j = j;
+  st.i = i;
+  if (i >= v.N) {
+    out = {v.N, 0.0f};
+    sm = 0.0;
+    return true;
+  }
+  return false;
+}
+
+}  // namespace nmg

@@ -1,0 +1,78 @@
+// Device-side description of one render: the sample grid, the per-row and
+// per-column tables the host computed in arbitrary precision, the FP64 copy
+// of the reference orbit and series, and the output grid.  Passed to every
+// kernel by value.
+#pragma once
+
+#include <cstdint>
+
+#if defined(__CUDACC__)
+#define NM_HD __host__ __device__ __forceinline__
+#else
+#define NM_HD inline
+#endif
+
+namespace nmg {
+
+// grid.h:8-14 -- one sample of the output grid, 8 bytes, row-major r*nc+c.
+struct EscapeValue {
+  int32_t iterations;
+  float smoothing;
+};
+
+struct Dbl2 {
+  double x, y;
+};
+
+enum CardioidMode : int32_t {
+  CARDIOID_PER_SAMPLE = 0,  // evaluate the test for each sample (double-double)
+  CARDIOID_NONE = 1,        // the view box is provably outside both regions
+};
+
+struct DeviceView {
+  int32_t nr, nc;          // sample grid
+  int32_t N;               // iteration count
+  int32_t cardioid_mode;
+  double tol;              // series error tolerance
+  double bailout2;         // 1024^2 (mandelbrot.cpp:58-59)
+  double log_bailout;      // log(1024), rounded on the host
+  int32_t tile_w, tile_h;  // sample order: tiles of tile_w x tile_h, row-major inside
+  int32_t tiles_x, tiles_y;
+  int32_t row0, row1;      // rows [row0, row1) of the grid take part in this launch
+  int64_t total;           // tiles_x * tiles_y * tile_w * tile_h (padded)
+
+  const Dbl2* coord_re;    // [nc] per column: pt.re = hi + lo
+  const Dbl2* coord_im;    // [nr] per row:    pt.im = hi + lo
+
+  // deep path (not the reference's hardware path)
+  const double* eps_re;    // [nc] get_d(pt.re - X[0].re)
+  const double* eps_im;    // [nr] get_d(pt.im - X[0].im)
+  const Dbl2* z;           // [zlen] 0, get_d(X[k]), escaped element
+  int32_t zlen;
+  int32_t xlen;            // X.size()
+  const Dbl2* xhi;         // [xlen] get_d(X[k])
+  const Dbl2* xlo;         // [xlen] get_d(X[k] - xhi)
+  const Dbl2* sa_a;        // [xlen] get_d(A[k])
+  const Dbl2* sa_b;
+  const Dbl2* sa_c;
+  const double* sa_min;    // [xlen] prefix min of tol |B_i|^2/|C_i|^2
+  int32_t sa_scan;         // 1: walk the series term by term (no threshold shortcut)
+  int32_t pad_;
+
+  EscapeValue* grid;       // [nr*nc]
+  double* smooth64;        // optional [nr*nc] unrounded smoothing
+};
+
+// Sample index in tile order -> (r, c); false for padding past the grid edge.
+NM_HD bool sample_rc(const DeviceView& v, int64_t s, int& r, int& c) {
+  const int64_t per_tile = (int64_t)v.tile_w * v.tile_h;
+  const int64_t tile = s / per_tile;
+  const int t = (int)(s - tile * per_tile);
+  const int ty = (int)(tile / v.tiles_x);
+  const int tx = (int)(tile - (int64_t)ty * v.tiles_x);
+  r = v.row0 + ty * v.tile_h + t / v.tile_w;
+  c = tx * v.tile_w + t % v.tile_w;
+  return r < v.row1 && c < v.nc;
+}
+
+}  // namespace nmg

@@ -1,0 +1,55 @@
+"""Views and small helpers shared by the tests."""
+from decimal import Decimal, getcontext
+
+import numpy as np
+
+
+def step_for(width, cols, digits=40):
+    """Pixel step width/cols as a decimal string (exact decimal division)."""
+    getcontext().prec = digits
+    return str(Decimal(str(width)) / Decimal(cols))
+
+
+# 640x480, center -0.75+0i, width 3.0, N 1024: the reference's double path.
+C1 = dict(nr=480, nc=640, sc=1, cre="-0.75", cim="0", step="0.0046875", N=1024, tol=1e-10)
+# 1920x1080 with 4x4 samples, width 1e-12, N 50,000: the arbitrary-precision path.
+C2 = dict(nr=1080, nc=1920, sc=4, cre="-0.743643887037151", cim="0.131825904205330",
+          step=step_for("1e-12", 1920), N=50000, tol=1e-10)
+
+
+def shrink(view, nr, nc, N=None):
+    """Same center and width at a smaller grid (for fast tests)."""
+    v = dict(view)
+    width = Decimal(view["step"]) * view["nc"]
+    v["nr"], v["nc"] = nr, nc
+    v["step"] = step_for(width, nc)
+    if N is not None:
+        v["N"] = N
+    return v
+
+
+def setup_oracle(oracle_mod, view):
+    o = oracle_mod.OracleView(view["nr"], view["nc"])
+    o.set_view(view["cre"], view["cim"], view["step"], view["step"], view["N"], view["tol"],
+               view.get("min_bits", 0))
+    if view["sc"] > 1:
+        o.scale_up(view["sc"])
+    return o
+
+
+def setup_gpu(nm, view, path=0, keep64=True):
+    m = nm.Mandelbrot(view["nr"], view["nc"])
+    m.set_view(view["cre"], view["cim"], view["step"], view["step"], view["N"], view["tol"],
+               view.get("min_bits", 0))
+    if view["sc"] > 1:
+        m.scaleUp(view["sc"])
+    m.set_path(path)
+    if keep64:
+        m.set_option(nm.OPT_KEEP_SMOOTH64, 1)
+    return m
+
+
+def sample_positions(nr, nc, n, seed):
+    rng = np.random.default_rng(seed)
+    k = rng.choice(nr * nc, size=min(n, nr * nc), replace=False)
+    return (k // nc).astype(np.int32), (k % nc).astype(np.int32)

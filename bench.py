@@ -192,6 +192,10 @@ def run_ours(args):
     m.precompute()
     precompute_s = time.perf_counter() - t0
     m.upload()
+    # the plain FP64 path on the same precomputed orbit (value copy)
+    fp = m.copy()
+    fp.set_path(nm.PATH_FP64)
+    fp.upload()
 
     def render_timed(mm, k, w):
         times = []
@@ -225,7 +229,25 @@ def run_ours(args):
     g = m.grid()
     eff_iters = int(g["iterations"].astype(np.int64).sum())
     executed = m.stat(nm.STAT_EXECUTED_ITERS)
+    rework = m.stat(nm.STAT_FP64_REWORK)
+    k_main_ms = m.stat(nm.STAT_KERNEL_NS) * 1e-6
+    k_rework_ms = m.stat(nm.STAT_REWORK_KERNEL_NS) * 1e-6
     value = eff_iters * world / (ms * 1e-3)
+
+    # the plain FP64 path: timed on the same workload, and the comparison grid
+    fp64_ms = None
+    if primary != nm.PATH_FP64:
+        render_timed(fp, 0, 1)
+        fp64_ms = float(np.mean(render_timed(fp, max(1, min(args.steps, 2)), 0)))
+    gf = fp.grid()
+    same = gf["iterations"] == g["iterations"]
+    exact = float(same.mean())
+    dsm = np.abs(gf["smoothing"].astype(np.float64) - g["smoothing"])
+    max_dsmooth_exact = float(dsm[same].max()) if same.any() else None
+    red_fe = m.reduce(SC)
+    red_fp = fp.reduce(SC)
+    exact_px = float((red_fe["iterations"] == red_fp["iterations"]).mean())
+    del gf, dsm, same
 
     # e2e through the C ABI with host buffers
     red = np.empty((NR, NC), nm.ESCAPE_DTYPE)
@@ -248,21 +270,33 @@ def run_ours(args):
         peak32 = nm.peak_flops(0)
         peak64 = nm.peak_flops(2)
         peak = peak32 if primary == nm.PATH_FE32 else peak64
-        achieved = executed * FLOPS_PER_ITER / (ms * 1e-3)
+        # dominant kernel: the FE32 (or FP64) render kernel, its own duration
+        main_ms = k_main_ms if k_main_ms > 0 else ms
+        achieved = executed * FLOPS_PER_ITER / (main_ms * 1e-3)
         line = {
             "metric": METRIC, "value": value, "unit": "pixel-iters/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "fp32+int-exponent" if primary == nm.PATH_FE32 else "fp64",
+            "dtype": "fp32 float-float + int exponent" if primary == nm.PATH_FE32 else "fp64",
             "data": "synthetic view (no dataset)", "config": workload_config(),
             "path": args.path,
+            "exact_iter_fraction_vs_fp64": exact, "exact_iter_fraction_reduced_px": exact_px,
+            "max_dsmooth_exact_samples": max_dsmooth_exact,
+            "fp64_rework_fraction": rework / float(NR * NC * SC * SC),
+            "fp64_path": None if fp64_ms is None else {
+                "ms_per_step": fp64_ms, "value": eff_iters / (fp64_ms * 1e-3),
+                "unit": "pixel-iters/s"},
+            "speedup_vs_fp64": None if fp64_ms is None else fp64_ms / ms,
+            "kernel_ms": {"render": k_main_ms, "fp64_rework": k_rework_ms},
             "executed_iters_per_step": executed, "effective_iters_per_step": eff_iters,
             "precompute_s": precompute_s, "wall_s": wall,
-            "gpu_launches": 2 * args.steps,
+            "gpu_launches": (3 if primary == nm.PATH_FE32 else 1) * args.steps,
             "roofline": {"bound": "fp32" if primary == nm.PATH_FE32 else "fp64",
                          "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
                          "frac": achieved / peak, "traffic": None,
-                         "peak_source": "measured by nm_peak_flops on this GPU"},
+                         "flops_per_iter": FLOPS_PER_ITER,
+                         "peak_source": "measured by nm_peak_flops on this GPU "
+                                        "(FP32 FMA / FP64 unfused mul+add issue rate)"},
             "clocks": clocks.summary(),
             "e2e": {"value": eff_iters / e2e_s, "unit": "pixel-iters/s",
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": NR * NC * 8},

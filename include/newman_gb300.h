@@ -69,11 +69,13 @@ enum nm_stat {
   NM_STAT_EXECUTED_ITERS = 1,     /* z^2 + c steps run on the GPU in the last render */
   NM_STAT_SAMPLES = 2,            /* samples finished in the last render */
   NM_STAT_REBASES = 3,            /* perturbation rebases in the last render */
-  NM_STAT_GLITCHES = 4,           /* FE32 steps re-checked in FP64 */
+  NM_STAT_FP64_REWORK = 4,        /* FE32 samples not certified, re-rendered in FP64 */
   NM_STAT_ORBIT_LENGTH = 16,      /* X.size() of the last precompute */
   NM_STAT_PROBE_INDEX = 17,       /* winning probe of findProbe */
   NM_STAT_PRECISION_BITS = 18,    /* arbitrary precision of the view */
-  NM_STAT_PRECOMPUTE_US = 19      /* host time of the last nm_precompute */
+  NM_STAT_PRECOMPUTE_US = 19,     /* host time of the last nm_precompute */
+  NM_STAT_KERNEL_NS = 20,         /* GPU time of the last render's main kernel */
+  NM_STAT_REWORK_KERNEL_NS = 21   /* GPU time of the last FE32 render's FP64 rework */
 };
 
 /* Mandelbrot::Mandelbrot(int nr, int nc), mandelbrot.cpp:8-17: center -0.5,

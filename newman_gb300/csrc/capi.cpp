@@ -69,6 +69,15 @@ struct DevBuf {
 
 static_assert(sizeof(nm_escape_value) == sizeof(EscapeValue), "grid layout");
 
+// Device scratch words of a handle: the persistent kernels' work counters and
+// statistics, and the length of the FE32 rework list.
+constexpr int kNextMain = 0;
+constexpr int kStatsMain = 1;
+constexpr int kNextRework = kStatsMain + nmg::STAT_COUNT;
+constexpr int kStatsRework = kNextRework + 1;
+constexpr int kReworkCount = kStatsRework + nmg::STAT_COUNT;
+constexpr int kScratchWords = kReworkCount + 1;
+
 }  // namespace
 
 struct nm_handle {
@@ -94,16 +103,24 @@ struct nm_handle {
   bool outside_cardioid = false;
   double precompute_us = 0.0;
   DevBuf<Dbl2> d_coord_re, d_coord_im, d_z, d_xhi, d_xlo, d_a, d_b, d_c;
+  DevBuf<nmg::Flt4> d_zf;
   DevBuf<double> d_eps_re, d_eps_im, d_sa_min;
 
-  // scratch: work counter + statistics
-  DevBuf<unsigned long long> d_scratch;
+  // scratch: work counters, statistics, and the FE32 rework list
+  DevBuf<unsigned long long> d_scratch;  // kScratchWords, layout below
+  DevBuf<unsigned int> d_rework;
   int* cancel_host = nullptr;
   int* cancel_dev = nullptr;
   long long expected_samples = 0;
+  // events around the last render's kernels: [0] before, [1] after the main
+  // kernel, [2] after the FE32 rework kernel
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+  bool timed_rework = false;
 
   nm_handle(int nr, int nc) : view(nr, nc) {}
   ~nm_handle() {
+    for (cudaEvent_t e : ev)
+      if (e) cudaEventDestroy(e);
     if (stream) cudaStreamDestroy(stream);
     if (cancel_host) cudaFreeHost(cancel_host);
   }
@@ -125,8 +142,9 @@ int ensure_device(nm_handle* h) {
   NM_CUDA(cudaHostAlloc(&h->cancel_host, sizeof(int), cudaHostAllocMapped));
   *h->cancel_host = 0;
   NM_CUDA(cudaHostGetDevicePointer((void**)&h->cancel_dev, h->cancel_host, 0));
-  NM_CUDA(h->d_scratch.reserve(1 + nmg::STAT_COUNT));
-  NM_CUDA(cudaMemsetAsync(h->d_scratch.p, 0, (1 + nmg::STAT_COUNT) * 8, h->stream));
+  NM_CUDA(h->d_scratch.reserve(kScratchWords));
+  NM_CUDA(cudaMemsetAsync(h->d_scratch.p, 0, kScratchWords * 8, h->stream));
+  for (cudaEvent_t& e : h->ev) NM_CUDA(cudaEventCreate(&e));
   return NM_OK;
 }
 
@@ -186,6 +204,12 @@ int do_upload(nm_handle* h) {
     if ((rc = upload(h->d_eps_re, h->eps_re, h->stream))) return rc;
     if ((rc = upload(h->d_eps_im, h->eps_im, h->stream))) return rc;
     if ((rc = upload(h->d_z, cv(h->od.z), h->stream))) return rc;
+    std::vector<nmg::Flt4> zf(h->od.z.size());
+    for (size_t k = 0; k < zf.size(); k++) {
+      const float hx = (float)h->od.z[k].x, hy = (float)h->od.z[k].y;
+      zf[k] = {hx, hy, (float)(h->od.z[k].x - hx), (float)(h->od.z[k].y - hy)};
+    }
+    if ((rc = upload(h->d_zf, zf, h->stream))) return rc;
     if ((rc = upload(h->d_xhi, cv(h->od.xhi), h->stream))) return rc;
     if ((rc = upload(h->d_xlo, cv(h->od.xlo), h->stream))) return rc;
     if ((rc = upload(h->d_a, cv(h->od.a), h->stream))) return rc;
@@ -357,7 +381,8 @@ int nm_get_stat(nm_handle* h, int stat, long long* value) {
       return NM_OK;
     }
     NM_CUDA(cudaStreamSynchronize(h->stream));
-    NM_CUDA(cudaMemcpy(&v, h->d_scratch.p + 1 + stat, 8, cudaMemcpyDeviceToHost));
+    const int slot = stat == nmg::STAT_REWORK ? kReworkCount : kStatsMain + stat;
+    NM_CUDA(cudaMemcpy(&v, h->d_scratch.p + slot, 8, cudaMemcpyDeviceToHost));
     *value = (long long)v;
     return NM_OK;
   }
@@ -366,6 +391,17 @@ int nm_get_stat(nm_handle* h, int stat, long long* value) {
     case NM_STAT_PROBE_INDEX: *value = h->precomputed ? h->od.probe_index : -1; return NM_OK;
     case NM_STAT_PRECISION_BITS: *value = (long long)h->view.bits(); return NM_OK;
     case NM_STAT_PRECOMPUTE_US: *value = (long long)h->precompute_us; return NM_OK;
+    case NM_STAT_KERNEL_NS:
+    case NM_STAT_REWORK_KERNEL_NS: {
+      *value = 0;
+      if (!h->stream || (stat == NM_STAT_REWORK_KERNEL_NS && !h->timed_rework)) return NM_OK;
+      cudaEvent_t a = stat == NM_STAT_KERNEL_NS ? h->ev[0] : h->ev[1];
+      cudaEvent_t b = stat == NM_STAT_KERNEL_NS ? h->ev[1] : h->ev[2];
+      if (cudaEventSynchronize(b) != cudaSuccess) return NM_OK;  // never recorded
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, a, b) == cudaSuccess) *value = (long long)(ms * 1e6);
+      return NM_OK;
+    }
   }
   return fail(NM_ERR_ARG, "unknown stat %d", stat);
 }
@@ -429,6 +465,7 @@ int nm_render_rows(nm_handle* h, int r0, int r1, void* stream_arg) {
     v.eps_re = h->d_eps_re.p;
     v.eps_im = h->d_eps_im.p;
     v.z = h->d_z.p;
+    v.zf = h->d_zf.p;
     v.zlen = (int)h->od.z.size();
     v.xlen = h->od.xlen;
     v.xhi = h->d_xhi.p;
@@ -445,14 +482,20 @@ int nm_render_rows(nm_handle* h, int r0, int r1, void* stream_arg) {
   nmg::KernelKind kind = hw ? nmg::KERNEL_HW
                        : (h->path == NM_PATH_FE32 ? nmg::KERNEL_FE32 : nmg::KERNEL_DELTA64);
   nmg::RenderCtl ctl;
-  ctl.next = h->d_scratch.p;
-  ctl.stats = h->d_scratch.p + 1;
+  std::memset(&ctl, 0, sizeof ctl);
+  ctl.next = h->d_scratch.p + kNextMain;
+  ctl.stats = h->d_scratch.p + kStatsMain;
   ctl.cancel = h->cancel_dev;
   ctl.first = 0;
   ctl.count = v.total;
+  if (kind == nmg::KERNEL_FE32) {
+    NM_CUDA(h->d_rework.reserve((size_t)v.total));
+    ctl.rework = h->d_rework.p;
+    ctl.rework_n = h->d_scratch.p + kReworkCount;
+  }
   *h->cancel_host = 0;
   h->expected_samples = (long long)(r1 - r0) * nc;
-  NM_CUDA(cudaMemsetAsync(h->d_scratch.p, 0, (1 + nmg::STAT_COUNT) * 8, s));
+  NM_CUDA(cudaMemsetAsync(h->d_scratch.p, 0, kScratchWords * 8, s));
   if (v.total == 0) return NM_OK;
   int blocks = h->blocks > 0 ? h->blocks : nmg::persistent_blocks(kind, h->device);
   long long max_useful = (v.total + 31) / 32;  // one warp per 32 samples at most
@@ -462,7 +505,25 @@ int nm_render_rows(nm_handle* h, int r0, int r1, void* stream_arg) {
   if (blocks < 1) blocks = 1;
   int chunk = h->chunk;
   if (kind == nmg::KERNEL_FE32) chunk = h->renorm;  // the FE32 kernel renormalises per chunk
+  NM_CUDA(cudaEventRecord(h->ev[0], s));
   NM_CUDA(nmg::launch_render(kind, v, ctl, s, blocks, chunk));
+  NM_CUDA(cudaEventRecord(h->ev[1], s));
+  h->timed_rework = kind == nmg::KERNEL_FE32;
+  if (kind == nmg::KERNEL_FE32) {
+    // Samples the FE32 kernel could not certify: the plain FP64 kernel
+    // renders them again, reading the list and its length from the GPU.
+    nmg::RenderCtl re = ctl;
+    re.next = h->d_scratch.p + kNextRework;
+    re.stats = h->d_scratch.p + kStatsRework;
+    re.list = h->d_rework.p;
+    re.count_ptr = h->d_scratch.p + kReworkCount;
+    re.count = 0;
+    re.rework = nullptr;
+    re.rework_n = nullptr;
+    int rblocks = h->blocks > 0 ? h->blocks : nmg::persistent_blocks(nmg::KERNEL_DELTA64, h->device);
+    NM_CUDA(nmg::launch_render(nmg::KERNEL_DELTA64, v, re, s, rblocks, h->chunk));
+    NM_CUDA(cudaEventRecord(h->ev[2], s));
+  }
   return NM_OK;
 }
 
@@ -472,7 +533,8 @@ int nm_synchronize(nm_handle* h) {
   NM_CUDA(cudaStreamSynchronize(h->stream));
   if (*h->cancel_host) {
     unsigned long long done = 0;
-    NM_CUDA(cudaMemcpy(&done, h->d_scratch.p + 1 + nmg::STAT_SAMPLES, 8, cudaMemcpyDeviceToHost));
+    NM_CUDA(cudaMemcpy(&done, h->d_scratch.p + kStatsMain + nmg::STAT_SAMPLES, 8,
+                       cudaMemcpyDeviceToHost));
     if ((long long)done < h->expected_samples)
       return fail(NM_ERR_CANCELLED, "render cancelled after %llu of %lld samples", done,
                   h->expected_samples);

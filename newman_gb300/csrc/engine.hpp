@@ -12,7 +12,7 @@ enum StatIndex {
   STAT_EXECUTED_ITERS = 1,      // z -> z^2 + c steps run on the GPU
   STAT_SAMPLES = 2,             // samples finished
   STAT_REBASES = 3,             // rebases of the perturbation delta
-  STAT_GLITCHES = 4,            // FP32 steps redone in FP64 near a threshold
+  STAT_REWORK = 4,              // samples the FE32 kernel handed to the FP64 kernel
   STAT_COUNT = 8
 };
 
@@ -24,6 +24,13 @@ struct RenderCtl {
   const volatile int* cancel;    // host-mapped flag, may be null
   long long first;               // first sample index (tile order)
   long long count;               // samples in this launch
+  // Work from a list instead of a range: item k is sample list[k], and the
+  // item count is read from device memory (written by an earlier kernel).
+  const unsigned int* list;
+  const unsigned long long* count_ptr;
+  // Samples whose escape count a kernel could not certify are appended here.
+  unsigned int* rework;
+  unsigned long long* rework_n;
 };
 
 enum KernelKind { KERNEL_HW = 0, KERNEL_DELTA64 = 1, KERNEL_FE32 = 2 };

@@ -7,6 +7,11 @@
 // Every loop is bounded: a sample runs at most N iterations and the counter
 // only grows, so the kernel always ends.  A host-set cancel flag stops the
 // hand-out of new samples; samples already started are finished.
+//
+// Work comes either as a range of sample indices in tile order or as a list
+// of sample indices whose length an earlier kernel wrote to device memory.
+// A job that certifies its results (Job::kCertifies) appends each sample it
+// could not certify to ctl.rework; its provisional result is still stored.
 #pragma once
 
 #include "engine.hpp"
@@ -30,8 +35,10 @@ __device__ __forceinline__ void persistent_loop(const DeviceView& v, const Rende
   typename Job::State st;
   bool active = false, exhausted = false;
   int r = 0, c = 0;
+  long long sid = 0;
   unsigned long long executed = 0, rebases = 0, finished = 0, undecided = 0;
-  const unsigned long long end = (unsigned long long)ctl.count;
+  const unsigned long long end =
+      ctl.count_ptr ? *ctl.count_ptr : (unsigned long long)ctl.count;
 
   for (;;) {
     // Refill every idle lane (a new sample may finish at once, e.g. inside
@@ -53,17 +60,20 @@ __device__ __forceinline__ void persistent_loop(const DeviceView& v, const Rende
             base == ~0ull ? ~0ull : base + __popc(need & ((1u << lane) - 1));
         if (mine >= end) {
           exhausted = true;
-        } else if (sample_rc(v, ctl.first + (long long)mine, r, c)) {
-          EscapeValue out;
-          double sm = 0.0;
-          bool und = false;
-          if (Job::init(v, r, c, st, out, sm, und)) {
-            store_sample(v, r, c, out, sm);
-            finished++;
-          } else {
-            active = true;
+        } else {
+          sid = ctl.list ? (long long)ctl.list[mine] : ctl.first + (long long)mine;
+          if (sample_rc(v, sid, r, c)) {
+            EscapeValue out;
+            double sm = 0.0;
+            bool und = false;
+            if (Job::init(v, r, c, st, out, sm, und)) {
+              store_sample(v, r, c, out, sm);
+              finished++;
+            } else {
+              active = true;
+            }
+            undecided += und ? 1 : 0;
           }
-          undecided += und ? 1 : 0;
         }
       }
     }
@@ -73,6 +83,10 @@ __device__ __forceinline__ void persistent_loop(const DeviceView& v, const Rende
       double sm = 0.0;
       if (Job::steps(v, st, chunk, out, sm, executed, rebases)) {
         store_sample(v, r, c, out, sm);
+        if (Job::kCertifies && !Job::certified(st)) {
+          const unsigned long long k = atomicAdd(ctl.rework_n, 1ull);
+          ctl.rework[k] = (unsigned int)sid;
+        }
         finished++;
         active = false;
       }

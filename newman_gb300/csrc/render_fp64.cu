@@ -12,6 +12,8 @@ namespace nmg {
 
 struct HwJob {
   using State = HwState;
+  static constexpr bool kCertifies = false;
+  static __device__ __forceinline__ bool certified(const State&) { return true; }
   static __device__ __forceinline__ bool init(const DeviceView& v, int r, int c, State& st,
                                               EscapeValue& out, double& sm, bool& und) {
     return hw_init(v, r, c, st, out, sm, und);
@@ -32,6 +34,8 @@ struct Delta64Job {
   struct State {
     DeltaState d;
   };
+  static constexpr bool kCertifies = false;
+  static __device__ __forceinline__ bool certified(const State&) { return true; }
   static __device__ __forceinline__ bool init(const DeviceView& v, int r, int c, State& st,
                                               EscapeValue& out, double& sm, bool& und) {
     SeriesFront f;

@@ -24,6 +24,10 @@ struct Dbl2 {
   double x, y;
 };
 
+struct alignas(16) Flt4 {
+  float x, y, z, w;
+};
+
 enum CardioidMode : int32_t {
   CARDIOID_PER_SAMPLE = 0,  // evaluate the test for each sample (double-double)
   CARDIOID_NONE = 1,        // the view box is provably outside both regions
@@ -48,6 +52,7 @@ struct DeviceView {
   const double* eps_re;    // [nc] get_d(pt.re - X[0].re)
   const double* eps_im;    // [nr] get_d(pt.im - X[0].im)
   const Dbl2* z;           // [zlen] 0, get_d(X[k]), escaped element
+  const Flt4* zf;          // [zlen] the same as float-float {hi.re, hi.im, lo.re, lo.im}
   int32_t zlen;
   int32_t xlen;            // X.size()
   const Dbl2* xhi;         // [xlen] get_d(X[k])

@@ -40,10 +40,14 @@ METRIC = "pixel-iters/s on 1 GB300: FP32-floatexp vs plain FP64, >=99.99% px exa
 FLOPS_PER_ITER = 18
 
 
-def step_string():
+def step_string_for(cols):
     from decimal import Decimal, getcontext
     getcontext().prec = 40
-    return str(Decimal(WIDTH) / Decimal(NC))
+    return str(Decimal(WIDTH) / Decimal(cols))
+
+
+def step_string():
+    return step_string_for(NC)
 
 
 def workload_config():
@@ -162,6 +166,7 @@ def run_reference(args):
 
 
 def run_ours(args):
+    global NR, NC
     import torch
     import newman_gb300 as nm
 
@@ -187,6 +192,19 @@ def run_ours(args):
         return m
 
     primary = nm.PATH_FE32 if args.path == "fe32" else nm.PATH_FP64
+    if args.profile:
+        # One render per path of a 1/div-size crop of the workload (same center
+        # and width, fewer samples): the case the ncu captures run on.
+        NR, NC = NR // args.profile, NC // args.profile
+        step = step_string_for(NC)
+        for path in (nm.PATH_FE32, nm.PATH_FP64):
+            mm = make(path)
+            mm.precompute()
+            mm.render()
+            print("profile case %dx%d samples, path %d: %.1f ms, rework %d" % (
+                mm.rows(), mm.cols(), path, mm.stat(nm.STAT_KERNEL_NS) * 1e-6,
+                mm.stat(nm.STAT_FP64_REWORK)))
+        return
     m = make(primary)
     t0 = time.perf_counter()
     m.precompute()
@@ -321,6 +339,8 @@ def main():
     ap.add_argument("--path", default="fe32", choices=["fe32", "fp64"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile", type=int, default=0,
+                    help="render each path once on a 1/DIV-size crop and exit (ncu case)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

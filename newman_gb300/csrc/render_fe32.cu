@@ -211,13 +211,21 @@ __device__ __forceinline__ bool fe_steps(const DeviceView& v, FeState& st, int s
     const float r2 = fmaf(yr, yr, yi * yi);
     ym = sqrtf(r2);
     const float zn1 = fabsf(z.hx) + fabsf(z.hy);
-    const float yerr = err + kUZ * zn1 + 0x1p-22f * (zn1 + fabsf(dr.h) + fabsf(di.h));
-    if (ym + 2.0f * yerr > kBailout && ym - 2.0f * yerr <= kBailout) certified = false;
-    if (r2 > lo_band) {
+    // error of Y = Z + delta held in float-float (the rebase value)
+    const float yerr = err + kUZ * zn1 + kU * (zn1 + fabsf(dr.h) + fabsf(di.h));
+    if (r2 <= lo_band) {
+      // |Y| is below the bailout by more than 2^-11 of it; the hi-part
+      // estimate ym is good to 2^-22 (|Z| + |delta|), so the test is decided
+      // unless the bound covers the whole gap
+      if (2.0f * (yerr + 0x1p-22f * (zn1 + fabsf(dr.h) + fabsf(di.h))) >= kBailout - ym)
+        certified = false;
+    } else {
       // escape decided on the accurate Y (FP64 from the float-float parts)
       const Dbl2 zd = v.z[j];
       const double ydr = zd.x + ff_to_double(dr), ydi = zd.y + ff_to_double(di);
       const double r2d = ydr * ydr + ydi * ydi;
+      const double ymd = sqrt(r2d);
+      if (fabs(ymd - 1024.0) <= 2.0 * (double)yerr + 1e-12 * ymd) certified = false;
       if (r2d > v.bailout2) {
         executed += (unsigned long long)(i + 1 - start);
         sm = smoothing_of(r2d, v.log_bailout);

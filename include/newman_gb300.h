@@ -149,6 +149,27 @@ int nm_zoom_at(nm_handle* h, float scale, int r, int c, int sc);   /* mandelbrot
 int nm_load_legacy(nm_handle* h, const char* path);                /* mandelbrot.cpp:19-35 */
 int nm_save(const nm_handle* h, const char* path);                 /* viewer.cpp:12-23 */
 
+/* Render the handle's view on the FP32-floatexp path into device memory the
+   caller owns, allocating nothing (no cudaMalloc, cudaFree or allocating
+   library call).  No counterpart in the reference.  It is for callers that
+   cannot allocate device memory when they render: code recording its GPU
+   work into a CUDA graph by stream capture, or a process whose device memory
+   belongs to another framework's allocator or to a fixed budget.
+   The handle's tables must already be on the GPU (nm_precompute, then
+   nm_upload -- those two calls do allocate).  `out` is a device array of
+   rows*cols nm_escape_value; `stream` a cudaStream_t (NULL: the legacy
+   default stream); the call is asynchronous.  The scratch the kernels need
+   (work counters, statistics, the list of samples re-rendered in FP64) is
+   one static device array of NM_NOALLOC_MAX_SAMPLES * 4 + 256 bytes per GPU,
+   held by every GPU that loads the library until the process exits; views
+   of more than NM_NOALLOC_MAX_SAMPLES samples are refused with NM_ERR_ARG.
+   The first call on a device looks the array up (cudaGetSymbolAddress):
+   make that first call before any stream capture.  All calls share the one
+   array, so calls whose kernels overlap on the GPU (other streams or
+   threads) race: serialise them. */
+#define NM_NOALLOC_MAX_SAMPLES 4194304
+int nm_render_fe32_noalloc(nm_handle* h, nm_escape_value* out, void* stream);
+
 /* Measured issue ceiling of the current GPU, in flop/s (no reference
    counterpart; the roofline denominator of the per-sample kernels).
    kind 0: FP32 FMA, 1: FP64 FMA, 2: FP64 unfused multiply + add. */

@@ -34,7 +34,7 @@ EXPORTS = (
     "nm_upload", "nm_compute_row", "nm_render_rows", "nm_render", "nm_synchronize", "nm_cancel",
     "nm_at", "nm_at_sc", "nm_scale_up", "nm_scale_down", "nm_reduce", "nm_get_grid",
     "nm_get_smoothing64", "nm_device_grid", "nm_point_at", "nm_translate", "nm_zoom",
-    "nm_zoom_at", "nm_load_legacy", "nm_save", "nm_peak_flops",
+    "nm_zoom_at", "nm_load_legacy", "nm_save", "nm_peak_flops", "nm_render_fe32_noalloc",
 )
 
 
@@ -101,6 +101,7 @@ def load_library(path=LIB_PATH):
         "nm_load_legacy": (i32, [vp, cp]),
         "nm_save": (i32, [vp, cp]),
         "nm_peak_flops": (i32, [i32, P(dbl)]),
+        "nm_render_fe32_noalloc": (i32, [vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -252,6 +253,12 @@ class Mandelbrot:
         out = np.empty((self.rows(), self.cols()), np.float64)
         _check(_lib.nm_get_smoothing64(self._h, out.ctypes.data))
         return out
+
+    def render_noalloc(self, out_ptr, stream=None):
+        """FP32-floatexp render into caller-owned device memory (rows*cols
+        escape values at `out_ptr`), allocating nothing; asynchronous on
+        `stream`.  Needs precompute() and upload() first."""
+        _check(_lib.nm_render_fe32_noalloc(self._h, out_ptr, stream))
 
     def reduce(self, sc, out=None):
         """scaleDown(sc)'s averaged grid, returned without changing the object."""

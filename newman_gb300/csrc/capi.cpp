@@ -735,3 +735,51 @@ int nm_save(const nm_handle* h, const char* path) {
 }
 
 }  // extern "C"
+
+namespace nmg {
+
+void noalloc_fail(const std::string& why) { g_last_error = why; }
+
+// The device view of a handle whose tables are already on the GPU, for the
+// allocation-free entry point (noalloc.cu): only reads the handle.
+int noalloc_view(nm_handle* h, DeviceView& v, int& device, std::string& why) {
+  if (!h->precomputed || !h->uploaded || !h->stream || !h->d_zf.p) {
+    why = "the view's tables are not on the GPU: call nm_precompute and nm_upload first";
+    return NM_ERR_STATE;
+  }
+  const int nr = h->view.rows(), nc = h->view.cols();
+  std::memset(&v, 0, sizeof v);
+  v.nr = nr;
+  v.nc = nc;
+  v.N = h->view.iterations();
+  v.cardioid_mode = h->outside_cardioid ? CARDIOID_NONE : CARDIOID_PER_SAMPLE;
+  v.tol = h->view.tolerance();
+  v.bailout2 = 1024.0 * 1024.0;
+  v.log_bailout = std::log(1024.0);
+  v.tile_w = h->tile_w;
+  v.tile_h = h->tile_h;
+  v.row0 = 0;
+  v.row1 = nr;
+  v.tiles_x = (nc + h->tile_w - 1) / h->tile_w;
+  v.tiles_y = (nr + h->tile_h - 1) / h->tile_h;
+  v.total = (long long)v.tiles_x * v.tiles_y * h->tile_w * h->tile_h;
+  v.coord_re = h->d_coord_re.p;
+  v.coord_im = h->d_coord_im.p;
+  v.eps_re = h->d_eps_re.p;
+  v.eps_im = h->d_eps_im.p;
+  v.z = h->d_z.p;
+  v.zf = h->d_zf.p;
+  v.zlen = (int)h->od.z.size();
+  v.xlen = h->od.xlen;
+  v.xhi = h->d_xhi.p;
+  v.xlo = h->d_xlo.p;
+  v.sa_a = h->d_a.p;
+  v.sa_b = h->d_b.p;
+  v.sa_c = h->d_c.p;
+  v.sa_min = h->d_sa_min.p;
+  v.sa_scan = h->od.sa_fp64_ok ? 0 : 1;
+  device = h->device;
+  return NM_OK;
+}
+
+}  // namespace nmg

@@ -1,0 +1,69 @@
+"""The allocation-free render entry point, nm_render_fe32_noalloc.
+
+Callers that cannot allocate device memory when they render -- code that
+records its GPU work by stream capture, or a process whose device memory is
+owned by another framework's allocator -- pass their own output buffer and
+get the FP32-floatexp render of a prepared handle, with the kernels' scratch
+taken from a static device array.  Its output must equal the allocating
+entry point's (nm_render on the same handle): escape counts exactly, float
+smoothing within 1e-6, on two calls in a row.
+
+This file sorts last so that a run stopping at its first failure has already
+run every other test.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from helpers import C2, setup_gpu, shrink
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def nm():
+    import newman_gb300
+    newman_gb300.load_library()
+    return newman_gb300
+
+
+def test_noalloc_matches_allocating_render(nm):
+    torch = pytest.importorskip("torch")
+    view = shrink(C2, 135, 240, N=20000)  # 540 x 960 samples
+    m = setup_gpu(nm, view, path=nm.PATH_FE32, keep64=False)
+    m.precompute()
+    m.upload()
+    m.render()
+    ref = m.grid().copy()
+    rows, cols = m.rows(), m.cols()
+
+    # caller-owned output: 8 bytes per sample
+    out = torch.empty(rows * cols * 2, dtype=torch.int32, device="cuda")
+    stream = torch.cuda.current_stream()
+    for call in range(2):
+        out.fill_(-7)
+        m.render_noalloc(ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(stream.cuda_stream))
+        stream.synchronize()
+        got = out.cpu().numpy().view(nm.ESCAPE_DTYPE).reshape(rows, cols)
+        assert np.array_equal(got["iterations"], ref["iterations"]), "call %d" % call
+        assert np.abs(got["smoothing"] - ref["smoothing"]).max() <= 1e-6, "call %d" % call
+
+    # a further call takes no device memory
+    torch.cuda.synchronize()
+    free_before = torch.cuda.mem_get_info()[0]
+    m.render_noalloc(ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(stream.cuda_stream))
+    stream.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free_before
+
+
+def test_noalloc_refuses_oversize_and_unprepared(nm):
+    big = nm.Mandelbrot(2048, 2049)  # 4,196,352 samples > 4,194,304
+    with pytest.raises(nm.NewmanError) as e:
+        big.render_noalloc(ctypes.c_void_p(1))
+    assert e.value.code == nm.NM_ERR_ARG
+    assert "4194304" in str(e.value)
+    small = nm.Mandelbrot(8, 8)
+    with pytest.raises(nm.NewmanError) as e:
+        small.render_noalloc(ctypes.c_void_p(1))
+    assert e.value.code == nm.NM_ERR_STATE

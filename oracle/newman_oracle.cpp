@@ -694,6 +694,38 @@ int nmo_render_pixels(nmo_view* h, int mode, long npix, const int32_t* rows, con
   return 0;
 }
 
+// d.size() after the series loop of getIterations (mandelbrot.cpp:163-181)
+// for each listed sample: the number of iterations the series skips.  -1 for
+// samples inside the cardioid / period-2 disk.
+int nmo_series_skip(nmo_view* h, long npix, const int32_t* rows, const int32_t* cols,
+                    int32_t* dsize) {
+  View* v = reinterpret_cast<View*>(h);
+  if (v->use_hardware() || !v->precomputed) return 3;
+  Scratch s(v->bits);
+  MP pr(v->bits), pi(v->bits), tmp(v->bits);
+  for (long k = 0; k < npix; k++) {
+    v->point_im(rows[k], pi, tmp);
+    v->point_re(cols[k], pr, tmp);
+    if (in_cardioid(pr, pi, s)) {
+      dsize[k] = -1;
+      continue;
+    }
+    mpf_sub(s.yr, pr, &v->X.re[0]);
+    mpf_sub(s.yi, pi, &v->X.im[0]);
+    LP eps{mpf_get_d(s.yr), mpf_get_d(s.yi)};
+    LP eps2 = sq(eps), eps3 = mul(eps, eps2);
+    size_t n = v->X.size(), ds = n;
+    for (size_t i = 1; i < n; i++)
+      if (sa_term(*v, i, eps, eps2, eps3).unstable) {
+        long good = (long)i - 3;
+        ds = (size_t)(good < 1 ? 1 : good);
+        break;
+      }
+    dsize[k] = (int32_t)ds;
+  }
+  return 0;
+}
+
 // Render rows [r0, r1) of the sample grid, row-major (computeRow, :269-283).
 int nmo_render_rows(nmo_view* h, int mode, int r0, int r1, int32_t* iters, double* smooth,
                     int threads) {

@@ -42,6 +42,8 @@ def lib():
         L.nmo_render_rows.argtypes = [vp, i32, i32, i32, P(ctypes.c_int32), P(dbl), i32]
         L.nmo_reduce.argtypes = [i32, i32, i32, P(ctypes.c_int32), P(ctypes.c_float),
                                  P(ctypes.c_int32), P(ctypes.c_float)]
+        L.nmo_series_skip.argtypes = [vp, ctypes.c_long, P(ctypes.c_int32), P(ctypes.c_int32),
+                                      P(ctypes.c_int32)]
         L.nmo_get_view.argtypes = [vp, i32, ctypes.c_char_p, i32]
         _lib = L
     return _lib
@@ -130,6 +132,17 @@ class OracleView:
         if rc:
             raise RuntimeError("nmo_render_rows failed: %d" % rc)
         return it.reshape(r1 - r0, self.cols), sm.reshape(r1 - r0, self.cols)
+
+    def series_skip(self, rows, cols):
+        """d.size() after the series loop for each sample (-1: cardioid)."""
+        rows = np.ascontiguousarray(rows, np.int32)
+        cols = np.ascontiguousarray(cols, np.int32)
+        out = np.zeros(rows.shape, np.int32)
+        rc = lib().nmo_series_skip(self._h, rows.size, _p(rows, ctypes.c_int32),
+                                   _p(cols, ctypes.c_int32), _p(out, ctypes.c_int32))
+        if rc:
+            raise RuntimeError("nmo_series_skip failed: %d" % rc)
+        return out
 
     def get_view(self):
         out = []

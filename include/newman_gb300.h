@@ -61,7 +61,8 @@ enum nm_option {
   NM_OPT_KEEP_SMOOTH64 = 3, /* 1: also keep the unrounded double smoothing */
   NM_OPT_THREADS = 4,     /* host threads for the probe search (0 = all) */
   NM_OPT_BLOCKS = 5,      /* persistent blocks (0 = fill the GPU) */
-  NM_OPT_RENORM = 6       /* FE32: steps between exponent renormalisations */
+  NM_OPT_RENORM = 6,      /* FE32: steps between exponent renormalisations */
+  NM_OPT_FE32_SINGLE_PASS = 7 /* FE32 in one persistent kernel (default: three passes) */
 };
 
 enum nm_stat {
@@ -75,7 +76,8 @@ enum nm_stat {
   NM_STAT_PRECISION_BITS = 18,    /* arbitrary precision of the view */
   NM_STAT_PRECOMPUTE_US = 19,     /* host time of the last nm_precompute */
   NM_STAT_KERNEL_NS = 20,         /* GPU time of the last render's main kernel */
-  NM_STAT_REWORK_KERNEL_NS = 21   /* GPU time of the last FE32 render's FP64 rework */
+  NM_STAT_REWORK_KERNEL_NS = 21,  /* GPU time of the last FE32 render's FP64 rework */
+  NM_STAT_ITER_KERNEL_NS = 22     /* GPU time of the last FE32 render's iteration pass */
 };
 
 /* Mandelbrot::Mandelbrot(int nr, int nc), mandelbrot.cpp:8-17: center -0.5,

@@ -76,7 +76,8 @@ constexpr int kStatsMain = 1;
 constexpr int kNextRework = kStatsMain + nmg::STAT_COUNT;
 constexpr int kStatsRework = kNextRework + 1;
 constexpr int kReworkCount = kStatsRework + nmg::STAT_COUNT;
-constexpr int kScratchWords = kReworkCount + 1;
+constexpr int kWorkCount = kReworkCount + 1;  // FE32 pass pipeline: samples to iterate
+constexpr int kScratchWords = kWorkCount + 1;
 
 }  // namespace
 
@@ -84,7 +85,7 @@ struct nm_handle {
   nmg::MPView view;
   int device = 0;
   int path = NM_PATH_REFERENCE;
-  int tile_w = 16, tile_h = 16, chunk = 32, blocks = 0, threads = 0, renorm = 16;
+  int tile_w = 16, tile_h = 16, chunk = 32, blocks = 0, threads = 0, renorm = 32;
   bool keep_smooth64 = false;
   cudaStream_t stream = nullptr;
 
@@ -113,9 +114,13 @@ struct nm_handle {
   int* cancel_dev = nullptr;
   long long expected_samples = 0;
   // events around the last render's kernels: [0] before, [1] after the main
-  // kernel, [2] after the FE32 rework kernel
-  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
-  bool timed_rework = false;
+  // kernel (or FE32 passes), [2] after the FE32 rework kernel, [3]/[4] around
+  // the FE32 iteration pass
+  cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  bool timed_rework = false, timed_iter = false;
+  bool fe_single_pass = false;  // FE32 in one persistent kernel instead of the passes
+  DevBuf<char> d_fe_state, d_fe_result;
+  DevBuf<unsigned int> d_work;
 
   nm_handle(int nr, int nc) : view(nr, nc) {}
   ~nm_handle() {
@@ -367,6 +372,9 @@ int nm_set_option(nm_handle* h, int opt, long long value) {
       if (value < 1 || value > 256) return fail(NM_ERR_ARG, "renorm interval %lld", value);
       h->renorm = (int)value;
       return NM_OK;
+    case NM_OPT_FE32_SINGLE_PASS:
+      h->fe_single_pass = value != 0;
+      return NM_OK;
   }
   return fail(NM_ERR_ARG, "unknown option %d", opt);
 }
@@ -392,11 +400,16 @@ int nm_get_stat(nm_handle* h, int stat, long long* value) {
     case NM_STAT_PRECISION_BITS: *value = (long long)h->view.bits(); return NM_OK;
     case NM_STAT_PRECOMPUTE_US: *value = (long long)h->precompute_us; return NM_OK;
     case NM_STAT_KERNEL_NS:
-    case NM_STAT_REWORK_KERNEL_NS: {
+    case NM_STAT_REWORK_KERNEL_NS:
+    case NM_STAT_ITER_KERNEL_NS: {
       *value = 0;
-      if (!h->stream || (stat == NM_STAT_REWORK_KERNEL_NS && !h->timed_rework)) return NM_OK;
-      cudaEvent_t a = stat == NM_STAT_KERNEL_NS ? h->ev[0] : h->ev[1];
-      cudaEvent_t b = stat == NM_STAT_KERNEL_NS ? h->ev[1] : h->ev[2];
+      if (!h->stream || (stat == NM_STAT_REWORK_KERNEL_NS && !h->timed_rework) ||
+          (stat == NM_STAT_ITER_KERNEL_NS && !h->timed_iter))
+        return NM_OK;
+      cudaEvent_t a = stat == NM_STAT_KERNEL_NS ? h->ev[0]
+                    : stat == NM_STAT_REWORK_KERNEL_NS ? h->ev[1] : h->ev[3];
+      cudaEvent_t b = stat == NM_STAT_KERNEL_NS ? h->ev[1]
+                    : stat == NM_STAT_REWORK_KERNEL_NS ? h->ev[2] : h->ev[4];
       if (cudaEventSynchronize(b) != cudaSuccess) return NM_OK;  // never recorded
       float ms = 0.f;
       if (cudaEventElapsedTime(&ms, a, b) == cudaSuccess) *value = (long long)(ms * 1e6);
@@ -506,7 +519,23 @@ int nm_render_rows(nm_handle* h, int r0, int r1, void* stream_arg) {
   int chunk = h->chunk;
   if (kind == nmg::KERNEL_FE32) chunk = h->renorm;  // the FE32 kernel renormalises per chunk
   NM_CUDA(cudaEventRecord(h->ev[0], s));
-  NM_CUDA(nmg::launch_render(kind, v, ctl, s, blocks, chunk));
+  h->timed_iter = false;
+  if (kind == nmg::KERNEL_FE32 && !h->fe_single_pass) {
+    // FE32 pass pipeline: FP64 front, FP32 iteration, FP64 smoothing
+    NM_CUDA(h->d_fe_state.reserve((size_t)v.total * nmg::kFeStateBytes));
+    NM_CUDA(h->d_fe_result.reserve((size_t)v.total * nmg::kFeResultBytes));
+    NM_CUDA(h->d_work.reserve((size_t)v.total));
+    nmg::FePassBuffers b;
+    b.state = reinterpret_cast<nmg::FeState*>(h->d_fe_state.p);
+    b.result = reinterpret_cast<nmg::FeResult*>(h->d_fe_result.p);
+    b.work = h->d_work.p;
+    b.work_n = h->d_scratch.p + kWorkCount;
+    NM_CUDA(nmg::launch_fe32_passes(v, b, ctl, s, h->device, h->blocks, chunk, h->ev[3],
+                                    h->ev[4]));
+    h->timed_iter = true;
+  } else {
+    NM_CUDA(nmg::launch_render(kind, v, ctl, s, blocks, chunk));
+  }
   NM_CUDA(cudaEventRecord(h->ev[1], s));
   h->timed_rework = kind == nmg::KERNEL_FE32;
   if (kind == nmg::KERNEL_FE32) {

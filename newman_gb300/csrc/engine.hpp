@@ -35,6 +35,25 @@ struct RenderCtl {
 
 enum KernelKind { KERNEL_HW = 0, KERNEL_DELTA64 = 1, KERNEL_FE32 = 2 };
 
+// Buffers of the FE32 pass pipeline (render_fe32.cu), one record per sample
+// index in tile order.
+struct FeState;
+struct FeResult;
+constexpr int kFeStateBytes = 64;
+constexpr int kFeResultBytes = 16;
+struct FePassBuffers {
+  FeState* state;              // start state written by the front pass
+  FeResult* result;            // escape iteration and |Y|^2 from the iteration pass
+  unsigned int* work;          // samples that need the iteration pass
+  unsigned long long* work_n;  // their count (device scratch)
+};
+
+// front pass -> iteration pass (persistent, events around it if given) ->
+// smoothing pass.  ctl carries the counters, the stats and the rework list.
+cudaError_t launch_fe32_passes(const DeviceView& v, const FePassBuffers& b, const RenderCtl& ctl,
+                               cudaStream_t stream, int device, int blocks, int chunk,
+                               cudaEvent_t iter_begin, cudaEvent_t iter_end);
+
 // Persistent, warp-refilled launches: every warp keeps its 32 lanes busy by
 // pulling new samples from `ctl.next` as lanes finish.
 cudaError_t launch_render(KernelKind kind, const DeviceView& v, const RenderCtl& ctl,

@@ -1,0 +1,279 @@
+// The FP32 floatexp delta iteration with its error bound, shared by the
+// single-pass FE32 kernel and the multi-pass FE32 pipeline (render_fe32.cu).
+//
+//     t = 2 Z[j] + delta;  delta = t * delta + eps;  j += 1;  Y = Z[j] + delta
+//
+// delta, eps and the reference orbit Z are float-float pairs (two FP32 words)
+// and, while |delta| < 2^-60, delta and eps share one int exponent E per
+// sample (delta = mantissa * 2^E), renormalised at the end of every chunk of
+// steps and whenever the mantissa passes 2^60.
+//
+// Certification.  Alongside delta the iteration propagates a bound on the
+// absolute error of delta against exact arithmetic from the same start,
+//     e' = 2|Y| e + e^2 + u (|t||delta| + |eps|) + u_z 2|Z||delta|,
+// u the float-float rounding, u_z the float-float representation of the FP64
+// orbit.  The FP64 path's own rounding is 2^-9 of that bound, so when every
+// bailout test of a sample is decided by more than twice the bound, both paths
+// take the same branch at every test and return the same escape count.  A
+// sample with a test inside the band ends "uncertified".  The escape test
+// itself is float-float (|Y|^2 compared with 2^20), so the iteration uses no
+// FP64 at all.
+#pragma once
+
+#include "engine.hpp"
+#include "ff32.cuh"
+#include "pixel_fp64.cuh"
+
+namespace nmg {
+
+constexpr int kFeScaledBelow = -60;   // delta kept as mantissa * 2^E below 2^-60
+constexpr float kFeU = 0x1p-44f;      // float-float rounding per step (generous)
+constexpr float kFeUZ = 0x1p-47f;     // float-float representation of Z
+constexpr float kFeBailout = 1024.0f;       // mandelbrot.cpp:58
+constexpr float kFeBailout2 = 1048576.0f;   // mandelbrot.cpp:59
+
+struct alignas(16) FeState {
+  FF dr, di;      // delta * 2^-E
+  FF er, ei;      // eps * 2^-E
+  float err;      // error bound of delta, in the same units
+  int32_t E;      // 0: unscaled
+  int32_t j, i;   // orbit index, iteration count (getIterations' i)
+  int32_t certified;
+  int32_t pad_[3];
+};
+
+// Finished sample: escape iteration (N: no escape) and |Y|^2 at the escape.
+struct alignas(16) FeResult {
+  int32_t it;
+  int32_t certified;
+  FF r2;
+};
+
+struct ZFF {  // reference orbit element, float-float
+  float hx, hy, lx, ly;
+};
+
+__device__ __forceinline__ ZFF fe_load_z(const DeviceView& v, int j) {
+  const Flt4 z = v.zf[j];
+  return ZFF{z.x, z.y, z.z, z.w};
+}
+
+// Start state from the FP64 series front (bit-identical to the FP64 path's).
+__device__ __forceinline__ void fe_start(const SeriesFront& f, FeState& st) {
+  const double m = fmax(fmax(fabs(f.dfound.re), fabs(f.dfound.im)),
+                        fmax(fabs(f.eps.re), fabs(f.eps.im)));
+  int E = 0;
+  if (m > 0.0 && m < 0x1p-60) E = ilogb(m);
+  st.E = E;
+  st.dr = ff_from_double(scalbn(f.dfound.re, -E));
+  st.di = ff_from_double(scalbn(f.dfound.im, -E));
+  st.er = ff_from_double(scalbn(f.eps.re, -E));
+  st.ei = ff_from_double(scalbn(f.eps.im, -E));
+  st.err = kFeU * (fabsf(st.dr.h) + fabsf(st.di.h));
+  st.j = f.dsize;
+  st.i = f.dsize;
+  st.certified = 1;
+}
+
+// x^2 + y^2 in float-float.
+__device__ __forceinline__ FF ff_norm2(FF x, FF y) {
+  const float p1 = x.h * x.h, e1 = fmaf(x.h, x.h, -p1);
+  const float p2 = y.h * y.h, e2 = fmaf(y.h, y.h, -p2);
+  const FF s = ff_two_sum(p1, p2);
+  float lo = s.l + e1 + e2;
+  lo = fmaf(2.0f * x.h, x.l, lo);
+  lo = fmaf(2.0f * y.h, y.l, lo);
+  return ff_fast_two_sum(s.h, lo);
+}
+
+// The bailout test on Y = Z + delta (unscaled, float-float).  Returns true
+// when |Y|^2 > 2^20; clears `certified` when the error bound `yerr` on |Y|
+// reaches across 1024.
+__device__ __forceinline__ bool fe_escape_test(FF yr, FF yi, float yerr, bool& certified,
+                                               FF& r2) {
+  r2 = ff_norm2(yr, yi);
+  const float d = (r2.h - kFeBailout2) + r2.l;  // r2.h - 2^20 is exact near 2^20
+  // | |Y| - 1024 | <= 2 yerr  <=>  | |Y|^2 - 2^20 | <= (2048 + 2 yerr) 2 yerr
+  if (fabsf(d) <= (2048.0f + 2.0f * yerr) * 2.0f * yerr + 0x1p-40f * r2.h) certified = false;
+  return d > 0.0f;
+}
+
+__device__ __forceinline__ void fe_renormalise(FeState& st) {
+  const float mag = fmaxf(fabsf(st.dr.h), fabsf(st.di.h));
+  if (!(mag > 0.0f)) return;
+  const int e = ilogbf(mag);
+  st.dr = ff_scale(st.dr, -e);
+  st.di = ff_scale(st.di, -e);
+  st.er = ff_scale(st.er, -e);
+  st.ei = ff_scale(st.ei, -e);
+  st.err = ldexpf(st.err, -e);
+  st.E += e;
+  if (st.E >= kFeScaledBelow) {  // large enough for plain FP32
+    st.dr = ff_scale(st.dr, st.E);
+    st.di = ff_scale(st.di, st.E);
+    st.er = ff_scale(st.er, st.E);
+    st.ei = ff_scale(st.ei, st.E);
+    st.err = ldexpf(st.err, st.E);
+    st.E = 0;
+  }
+}
+
+// Steps while delta is scaled: Y = Z to working precision, so the events are
+// the reference's own escape, the end of the orbit, and Z passing so close to
+// 0 that |Y| < |delta| could hold (left to the FP64 kernel: uncertified).
+__device__ __forceinline__ bool fe_scaled_steps(const DeviceView& v, FeState& st, int steps,
+                                             FeResult& res, unsigned long long& executed,
+                                             unsigned long long& rebases) {
+  const int zlast = v.zlen - 1;
+  const int stop = min(v.N, st.i + steps);
+  const int start = st.i;
+  ZFF z = fe_load_z(v, st.j);
+  bool done = false;
+  for (; st.i < stop; st.i++) {
+    const FF sd_r = st.E < -140 ? FF{0.f, 0.f} : ff_scale(st.dr, st.E);
+    const FF sd_i = st.E < -140 ? FF{0.f, 0.f} : ff_scale(st.di, st.E);
+    const FF tr = ff_add(FF{2.0f * z.hx, 2.0f * z.lx}, sd_r);
+    const FF ti = ff_add(FF{2.0f * z.hy, 2.0f * z.ly}, sd_i);
+    const float zl1 = fabsf(z.hx) + fabsf(z.hy), dl1 = fabsf(st.dr.h) + fabsf(st.di.h);
+    FF nr, ni;
+    ff_cmul_add(tr, ti, st.dr, st.di, st.er, st.ei, nr, ni);
+    st.err = fmaf(2.0f * zl1, st.err,
+                  kFeU * fmaf(fabsf(tr.h) + fabsf(ti.h), dl1, fabsf(st.er.h) + fabsf(st.ei.h)) +
+                      kFeUZ * 2.0f * zl1 * dl1);
+    st.dr = nr;
+    st.di = ni;
+    st.j++;
+    z = fe_load_z(v, st.j);
+    const float zm2 = fmaf(z.hx, z.hx, z.hy * z.hy);
+    const FF yr = ff_add(FF{z.hx, z.lx}, st.E < -140 ? FF{0.f, 0.f} : ff_scale(st.dr, st.E));
+    const FF yi = ff_add(FF{z.hy, z.ly}, st.E < -140 ? FF{0.f, 0.f} : ff_scale(st.di, st.E));
+    if (zm2 > kFeBailout2 * (1.0f - 0x1p-10f)) {
+      const float yerr = ldexpf(st.err, st.E) + kFeUZ * (fabsf(z.hx) + fabsf(z.hy));
+      bool cert = st.certified != 0;
+      FF r2;
+      if (fe_escape_test(yr, yi, yerr, cert, r2)) {
+        st.certified = cert ? 1 : 0;
+        res.it = st.i;
+        res.r2 = r2;
+        done = true;
+        st.i++;
+        break;
+      }
+      st.certified = cert ? 1 : 0;
+    }
+    const float dmag = ldexpf(dl1, st.E);
+    if (fabsf(z.hx) + fabsf(z.hy) <= 4.0f * dmag) st.certified = 0;  // |Y| < |delta| possible
+    if (st.j == zlast) {  // orbit exhausted: rebase to Z[0], now unscaled
+      const float e_abs = ldexpf(st.err, st.E) + kFeUZ * 2048.0f + kFeU * (zl1 + dmag);
+      st.dr = yr;
+      st.di = yi;
+      st.er = ff_scale(st.er, st.E);
+      st.ei = ff_scale(st.ei, st.E);
+      st.err = e_abs;
+      st.E = 0;
+      st.j = 0;
+      rebases++;
+      st.i++;
+      break;
+    }
+    if (fmaxf(fabsf(st.dr.h), fabsf(st.di.h)) > 0x1p60f) {
+      st.i++;
+      break;
+    }
+  }
+  executed += (unsigned long long)(st.i - start);
+  if (!done && st.E != 0) fe_renormalise(st);
+  if (done) return true;
+  if (st.i >= v.N) {
+    res.it = v.N;
+    res.r2 = FF{0.f, 0.f};
+    return true;
+  }
+  return false;
+}
+
+// Up to `steps` iterations; true when the sample is finished (res filled,
+// st.certified final).
+__device__ __forceinline__ bool fe_advance(const DeviceView& v, FeState& st, int steps,
+                                           FeResult& res, unsigned long long& executed,
+                                           unsigned long long& rebases) {
+  if (st.E != 0) return fe_scaled_steps(v, st, steps, res, executed, rebases);
+  const int zlast = v.zlen - 1;
+  const int stop = min(v.N, st.i + steps);
+  const int start = st.i;
+  const float lo_band = kFeBailout2 * (1.0f - 0x1p-10f);
+  const float eps_l1 = fabsf(st.er.h) + fabsf(st.ei.h);
+  const FF er = st.er, ei = st.ei;
+  FF dr = st.dr, di = st.di;
+  float err = st.err;
+  int j = st.j, i = st.i;
+  bool certified = st.certified != 0;
+  ZFF z = fe_load_z(v, j);
+  // |Y| of the current state (for the error bound's amplification 2|Y|)
+  float ym = sqrtf(fmaf(z.hx + dr.h, z.hx + dr.h, (z.hy + di.h) * (z.hy + di.h)));
+  bool done = false;
+  for (; i < stop; i++) {
+    const FF tr = ff_add(FF{2.0f * z.hx, 2.0f * z.lx}, dr);
+    const FF ti = ff_add(FF{2.0f * z.hy, 2.0f * z.ly}, di);
+    const float zl1 = fabsf(z.hx) + fabsf(z.hy), dl1 = fabsf(dr.h) + fabsf(di.h);
+    const float ym_up = ym + 0x1p-22f * (zl1 + dl1);
+    err = fmaf(2.0f * ym_up + err, err,
+               kFeU * fmaf(fabsf(tr.h) + fabsf(ti.h), dl1, eps_l1) + kFeUZ * 2.0f * zl1 * dl1);
+    FF nr, ni;
+    ff_cmul_add(tr, ti, dr, di, er, ei, nr, ni);
+    dr = nr;
+    di = ni;
+    j++;
+    z = fe_load_z(v, j);
+    const float yr = z.hx + dr.h, yi = z.hy + di.h;
+    const float r2 = fmaf(yr, yr, yi * yi);
+    ym = sqrtf(r2);
+    const float zn1 = fabsf(z.hx) + fabsf(z.hy), dn1 = fabsf(dr.h) + fabsf(di.h);
+    // error of Y = Z + delta held in float-float (the rebase value)
+    const float yerr = err + kFeUZ * zn1 + kFeU * (zn1 + dn1);
+    if (r2 <= lo_band) {
+      // |Y| is below the bailout by more than 2^-11 of it; the hi-part
+      // estimate ym is good to 2^-22 (|Z| + |delta|), so the test is decided
+      // unless the bound covers the whole gap
+      if (2.0f * (yerr + 0x1p-22f * (zn1 + dn1)) >= kFeBailout - ym) certified = false;
+    } else {
+      FF r2ff;
+      if (fe_escape_test(ff_add(FF{z.hx, z.lx}, dr), ff_add(FF{z.hy, z.ly}, di), yerr,
+                         certified, r2ff)) {
+        res.it = i;
+        res.r2 = r2ff;
+        done = true;
+        i++;
+        break;
+      }
+    }
+    const float d2 = fmaf(dr.h, dr.h, di.h * di.h);
+    if (r2 < d2 || j == zlast) {  // rebase to Z[0]: delta = Y in float-float
+      const FF nyr = ff_add(FF{z.hx, z.lx}, dr);
+      const FF nyi = ff_add(FF{z.hy, z.ly}, di);
+      dr = nyr;
+      di = nyi;
+      err = yerr;
+      j = 0;
+      z = fe_load_z(v, 0);
+      ym = sqrtf(fmaf(dr.h, dr.h, di.h * di.h));
+      rebases++;
+    }
+  }
+  executed += (unsigned long long)(i - start);
+  st.dr = dr;
+  st.di = di;
+  st.err = err;
+  st.j = j;
+  st.i = i;
+  st.certified = certified ? 1 : 0;
+  if (done) return true;
+  if (i >= v.N) {
+    res.it = v.N;
+    res.r2 = FF{0.f, 0.f};
+    return true;
+  }
+  return false;
+}
+
+}  // namespace nmg

@@ -106,6 +106,11 @@ struct nm_handle {
   DevBuf<Dbl2> d_coord_re, d_coord_im, d_z, d_xhi, d_xlo, d_a, d_b, d_c;
   DevBuf<nmg::Flt4> d_zf;
   DevBuf<double> d_eps_re, d_eps_im, d_sa_min;
+  // floatexp tables (views outside the FP64 range)
+  std::vector<nmg::RFE> eps_re_fe, eps_im_fe;
+  DevBuf<nmg::RFE> d_eps_re_fe, d_eps_im_fe, d_sa_min_fe;
+  DevBuf<nmg::CFE> d_a_fe, d_b_fe, d_c_fe;
+  int reference_mode = nmg::REFERENCE_PROBES;
 
   // scratch: work counters, statistics, and the FE32 rework list
   DevBuf<unsigned long long> d_scratch;  // kScratchWords, layout below
@@ -221,6 +226,14 @@ int do_upload(nm_handle* h) {
     if ((rc = upload(h->d_b, cv(h->od.b), h->stream))) return rc;
     if ((rc = upload(h->d_c, cv(h->od.c), h->stream))) return rc;
     if ((rc = upload(h->d_sa_min, h->od.sa_min, h->stream))) return rc;
+    if (!h->od.sa_fp64_ok) {
+      if ((rc = upload(h->d_eps_re_fe, h->eps_re_fe, h->stream))) return rc;
+      if ((rc = upload(h->d_eps_im_fe, h->eps_im_fe, h->stream))) return rc;
+      if ((rc = upload(h->d_a_fe, h->od.a_fe, h->stream))) return rc;
+      if ((rc = upload(h->d_b_fe, h->od.b_fe, h->stream))) return rc;
+      if ((rc = upload(h->d_c_fe, h->od.c_fe, h->stream))) return rc;
+      if ((rc = upload(h->d_sa_min_fe, h->od.sa_min_fe, h->stream))) return rc;
+    }
   }
   // The vectors above are pageable; the copies are complete when the stream
   // reaches this point, so wait before the host may touch them again.
@@ -232,6 +245,19 @@ int do_upload(nm_handle* h) {
 int check_handle(const nm_handle* h) {
   if (!h) return fail(NM_ERR_ARG, "null handle");
   return NM_OK;
+}
+
+// Views outside the FP64 range run their series front in floatexp.
+void set_fe_tables(const nm_handle* h, nmg::DeviceView& v) {
+  v.sa_scan = 0;
+  v.sa_fe = h->od.sa_fp64_ok ? 0 : 1;
+  if (!v.sa_fe) return;
+  v.eps_re_fe = h->d_eps_re_fe.p;
+  v.eps_im_fe = h->d_eps_im_fe.p;
+  v.sa_a_fe = h->d_a_fe.p;
+  v.sa_b_fe = h->d_b_fe.p;
+  v.sa_c_fe = h->d_c_fe.p;
+  v.sa_min_fe = h->d_sa_min_fe.p;
 }
 
 }  // namespace
@@ -267,6 +293,10 @@ nm_handle* nm_copy(const nm_handle* src) {
   h->coord_im = src->coord_im;
   h->eps_re = src->eps_re;
   h->eps_im = src->eps_im;
+  h->eps_re_fe = src->eps_re_fe;
+  h->eps_im_fe = src->eps_im_fe;
+  h->reference_mode = src->reference_mode;
+  h->fe_single_pass = src->fe_single_pass;
   h->od = src->od;
   h->precomputed = src->precomputed;
   h->coords_valid = src->coords_valid;
@@ -375,6 +405,13 @@ int nm_set_option(nm_handle* h, int opt, long long value) {
     case NM_OPT_FE32_SINGLE_PASS:
       h->fe_single_pass = value != 0;
       return NM_OK;
+    case NM_OPT_REFERENCE:
+      if (value != nmg::REFERENCE_PROBES && value != nmg::REFERENCE_CENTER)
+        return fail(NM_ERR_ARG, "reference mode %lld", value);
+      h->reference_mode = (int)value;
+      h->precomputed = false;
+      h->uploaded = false;
+      return NM_OK;
   }
   return fail(NM_ERR_ARG, "unknown option %d", opt);
 }
@@ -427,8 +464,10 @@ int nm_precompute(nm_handle* h) {
   h->precomputed = false;
   if (!h->view.use_hardware() || h->path != NM_PATH_REFERENCE) {
     int threads = h->threads > 0 ? h->threads : (int)std::thread::hardware_concurrency();
-    if (h->view.precompute(threads, h->od)) return fail(NM_ERR_STATE, "precompute failed");
+    if (h->view.precompute(threads, h->od, h->reference_mode))
+      return fail(NM_ERR_STATE, "precompute failed");
     h->view.eps_tables(h->od, h->eps_re, h->eps_im);
+    if (!h->od.sa_fp64_ok) h->view.eps_tables_fe(h->eps_re_fe, h->eps_im_fe);
     h->precomputed = true;
   }
   h->precompute_us =
@@ -487,7 +526,7 @@ int nm_render_rows(nm_handle* h, int r0, int r1, void* stream_arg) {
     v.sa_b = h->d_b.p;
     v.sa_c = h->d_c.p;
     v.sa_min = h->d_sa_min.p;
-    v.sa_scan = h->od.sa_fp64_ok ? 0 : 1;
+    set_fe_tables(h, v);
   }
   v.grid = h->grid.p;
   v.smooth64 = h->keep_smooth64 ? h->smooth64.p : nullptr;
@@ -806,7 +845,7 @@ int noalloc_view(nm_handle* h, DeviceView& v, int& device, std::string& why) {
   v.sa_b = h->d_b.p;
   v.sa_c = h->d_c.p;
   v.sa_min = h->d_sa_min.p;
-  v.sa_scan = h->od.sa_fp64_ok ? 0 : 1;
+  set_fe_tables(h, v);
   device = h->device;
   return NM_OK;
 }

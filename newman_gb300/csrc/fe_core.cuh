@@ -22,7 +22,7 @@
 
 #include "engine.hpp"
 #include "ff32.cuh"
-#include "pixel_fp64.cuh"
+#include "pixel_fe64.cuh"
 
 namespace nmg {
 
@@ -60,15 +60,18 @@ __device__ __forceinline__ ZFF fe_load_z(const DeviceView& v, int j) {
 
 // Start state from the FP64 series front (bit-identical to the FP64 path's).
 __device__ __forceinline__ void fe_start(const SeriesFront& f, FeState& st) {
-  const double m = fmax(fmax(fabs(f.dfound.re), fabs(f.dfound.im)),
-                        fmax(fabs(f.eps.re), fabs(f.eps.im)));
-  int E = 0;
-  if (m > 0.0 && m < 0x1p-60) E = ilogb(m);
+  // exponent of the larger of |d[found]| and |eps| (their mantissas carry
+  // their own exponents d_e, eps_e in floatexp views)
+  const double dm = fmax(fabs(f.dfound.re), fabs(f.dfound.im));
+  const double em = fmax(fabs(f.eps.re), fabs(f.eps.im));
+  const int kNone = -(1 << 30);
+  const int mag = max(dm > 0.0 ? ilogb(dm) + f.d_e : kNone, em > 0.0 ? ilogb(em) + f.eps_e : kNone);
+  const int E = (mag > kNone && mag < -60) ? mag : 0;
   st.E = E;
-  st.dr = ff_from_double(scalbn(f.dfound.re, -E));
-  st.di = ff_from_double(scalbn(f.dfound.im, -E));
-  st.er = ff_from_double(scalbn(f.eps.re, -E));
-  st.ei = ff_from_double(scalbn(f.eps.im, -E));
+  st.dr = ff_from_double(scalbn(f.dfound.re, f.d_e - E));
+  st.di = ff_from_double(scalbn(f.dfound.im, f.d_e - E));
+  st.er = ff_from_double(scalbn(f.eps.re, f.eps_e - E));
+  st.ei = ff_from_double(scalbn(f.eps.im, f.eps_e - E));
   st.err = kFeU * (fabsf(st.dr.h) + fabsf(st.di.h));
   st.j = f.dsize;
   st.i = f.dsize;

@@ -290,18 +290,62 @@ void MPView::eps_tables(const OrbitData&, std::vector<double>& er, std::vector<d
   }
 }
 
-int MPView::precompute(int threads, OrbitData& od) {
-  od = OrbitData();
-  // Probe points of findProbe (mandelbrot.cpp:77-83), in the reference's order.
-  std::vector<std::pair<int, int>> pts;
-  for (int c = 0; c < nc_; c += 2) {
-    pts.push_back({nr_ / 4, c});
-    pts.push_back({nr_ / 2, c});
-    pts.push_back({3 * nr_ / 4, c});
+void MPView::eps_tables_fe(std::vector<RFE>& er, std::vector<RFE>& ei) const {
+  er.resize(nc_);
+  ei.resize(nr_);
+  Mpf p(bits_), t(bits_);
+  long e = 0;
+  for (int c = 0; c < nc_; c++) {
+    coord_re(c, p, t);
+    mpf_sub(t.p(), p.p(), x0re_.p());
+    const double m = mpf_get_d_2exp(&e, t.p());
+    er[c] = {m, m == 0.0 ? 0 : (int32_t)e};
   }
-  for (int r = 0; r < nr_; r += 2) pts.push_back({r, nc_ / 2});
+  for (int r = 0; r < nr_; r++) {
+    coord_im(r, p, t);
+    mpf_sub(t.p(), p.p(), x0im_.p());
+    const double m = mpf_get_d_2exp(&e, t.p());
+    ei[r] = {m, m == 0.0 ? 0 : (int32_t)e};
+  }
+}
 
-  std::vector<int> len(pts.size(), 0);
+// get_d of a complex mpf value as a floatexp pair with one exponent: the same
+// truncated mantissas mpf_get_d_2exp returns, rescaled exactly.
+static CFE cfe_of(mpf_srcptr re, mpf_srcptr im) {
+  long er = 0, ei = 0;
+  const double dr = mpf_get_d_2exp(&er, re), di = mpf_get_d_2exp(&ei, im);
+  if (dr == 0.0 && di == 0.0) return {0.0, 0.0, 0};
+  const long e = dr == 0.0 ? ei : di == 0.0 ? er : std::max(er, ei);
+  return {std::ldexp(dr, (int)(er - e)), std::ldexp(di, (int)(ei - e)), (int32_t)e};
+}
+
+static bool rfe_less_host(RFE x, RFE y) {
+  if (!(x.m > 0.0)) return y.m > 0.0 || (x.m < y.m);
+  if (!(y.m > 0.0)) return false;
+  if (std::isinf(x.m) || std::isinf(y.m)) return x.m < y.m;
+  const int ex = std::ilogb(x.m) + x.e, ey = std::ilogb(y.m) + y.e;
+  if (ex != ey) return ex < ey;
+  return std::scalbn(x.m, x.e - ex) < std::scalbn(y.m, y.e - ey);
+}
+
+int MPView::precompute(int threads, OrbitData& od, int reference_mode) {
+  od = OrbitData();
+  // Probe points of findProbe (mandelbrot.cpp:77-83), in the reference's order,
+  // or the view center alone: pointAt(nr/2 - 1, nc/2) is exactly the center.
+  std::vector<std::pair<int, int>> pts;
+  if (reference_mode == REFERENCE_CENTER) {
+    pts.push_back({nr_ / 2 - 1, nc_ / 2});
+  } else {
+    for (int c = 0; c < nc_; c += 2) {
+      pts.push_back({nr_ / 4, c});
+      pts.push_back({nr_ / 2, c});
+      pts.push_back({3 * nr_ / 4, c});
+    }
+    for (int r = 0; r < nr_; r += 2) pts.push_back({r, nc_ / 2});
+  }
+
+  std::vector<int> len(pts.size(), N_);
+  if (pts.size() > 1) {
   std::atomic<size_t> next{0};
   auto worker = [&]() {
     Mpf pr(bits_), pi(bits_), tmp(bits_);
@@ -318,13 +362,13 @@ int MPView::precompute(int threads, OrbitData& od) {
   for (int t = 1; t < T; t++) pool.emplace_back(worker);
   worker();
   for (auto& t : pool) t.join();
-  // Longest orbit wins, earliest probe on ties (the strict '>' at :90).
+  }
+  // Longest orbit wins, earliest probe on ties (the strict '>' at :90).  With
+  // a single probe its length is found by the orbit loop below.
   int best = 0;
   for (size_t k = 1; k < pts.size(); k++)
     if (len[k] > len[best]) best = (int)k;
   od.probe_index = best;
-  const int xlen = len[best];
-  od.xlen = xlen;
 
   // Orbit and series of the winner in one pass: X[i] (mandelbrot.cpp:102-103)
   // then A[i], B[i], C[i] from X[i-1] (mandelbrot.cpp:122-129).
@@ -345,12 +389,8 @@ int MPView::precompute(int threads, OrbitData& od) {
   mpf_set_d(bi.p(), 0.0);
   mpf_set_d(c_r.p(), 0.0);
   mpf_set_d(c_i.p(), 0.0);
-  od.z.reserve(xlen + 2);
-  od.xhi.resize(xlen);
-  od.xlo.resize(xlen);
-  od.a.resize(xlen);
-  od.b.resize(xlen);
-  od.c.resize(xlen);
+  const size_t cap = (size_t)std::min(N_, 1 << 20) + 2;
+  od.z.reserve(cap);
   od.z.push_back({0.0, 0.0});
   auto split = [&](mpf_srcptr v, double& hi, double& lo) {
     hi = mpf_get_d(v);
@@ -359,14 +399,28 @@ int MPView::precompute(int threads, OrbitData& od) {
     lo = mpf_get_d(s.t3.p());
   };
   mpf_ptr t1 = s.t1.p(), t2 = s.t2.p();
-  for (int i = 0; i < xlen; i++) {
-    split(xr.p(), od.xhi[i].x, od.xlo[i].x);
-    split(xi.p(), od.xhi[i].y, od.xlo[i].y);
-    od.z.push_back(od.xhi[i]);
-    od.a[i] = {ar.d(), ai.d()};
-    od.b[i] = {br.d(), bi.d()};
-    od.c[i] = {c_r.d(), c_i.d()};
-    if (i + 1 < xlen) {
+  bool escaped = false;
+  for (int i = 0;; i++) {
+    D2 hi, lo;
+    split(xr.p(), hi.x, lo.x);
+    split(xi.p(), hi.y, lo.y);
+    od.xhi.push_back(hi);
+    od.xlo.push_back(lo);
+    od.z.push_back(hi);
+    od.a.push_back({ar.d(), ai.d()});
+    od.b.push_back({br.d(), bi.d()});
+    od.c.push_back({c_r.d(), c_i.d()});
+    od.a_fe.push_back(cfe_of(ar.p(), ai.p()));
+    od.b_fe.push_back(cfe_of(br.p(), bi.p()));
+    od.c_fe.push_back(cfe_of(c_r.p(), c_i.p()));
+    if (i + 1 >= N_) break;  // X.resize(N) is full
+    // X[i+1]; computeOrbit stops at the first element that bails out
+    square_add(nxr.p(), nxi.p(), xr.p(), xi.p(), cr.p(), ci.p(), s);
+    if (bailed_out(nxr.p(), nxi.p())) {
+      escaped = true;
+      break;
+    }
+    {
       // A[i+1].re = 2.0 * (X.re * A.re - X.im * A.im) + 1.0
       mpf_mul(t1, xr.p(), ar.p()); mpf_mul(t2, xi.p(), ai.p()); mpf_sub(t1, t1, t2);
       mpf_mul(t1, s.two.p(), t1); mpf_add(nar.p(), t1, s.one.p());
@@ -396,13 +450,12 @@ int MPView::precompute(int threads, OrbitData& od) {
       br.swap(nbr); bi.swap(nbi);
       c_r.swap(ncr); c_i.swap(nci);
     }
-    if (i + 1 < xlen || xlen < N_) {
-      square_add(nxr.p(), nxi.p(), xr.p(), xi.p(), cr.p(), ci.p(), s);
-      xr.swap(nxr);
-      xi.swap(nxi);
-    }
+    xr.swap(nxr);
+    xi.swap(nxi);
   }
-  if (xlen < N_) od.z.push_back({xr.d(), xi.d()});  // the element that escaped
+  const int xlen = (int)od.xhi.size();
+  od.xlen = xlen;
+  if (escaped) od.z.push_back({nxr.d(), nxi.d()});  // the element that escaped
 
   // Series instability thresholds: term i fires when tol |b|^2 < |c|^2, which
   // in exact arithmetic is  tol |B_i|^2 / |C_i|^2 < |eps3|^2 / |eps2|^2.
@@ -424,6 +477,22 @@ int MPView::precompute(int threads, OrbitData& od) {
   double e_min = std::min(std::fabs(sre_.d()), std::fabs(sim_.d()));
   od.sa_fp64_ok = std::isfinite(bmax) && std::isfinite(cmax) && cmax * w * w * w < 1e140 &&
                   bmax * w * w < 1e140 && e_min > 1e-45;
+
+  // The same thresholds in floatexp, for views outside the FP64 range.
+  od.sa_min_fe.assign(xlen, RFE{INFINITY, 0});
+  RFE runf{INFINITY, 0};
+  for (int i = 1; i < xlen; i++) {
+    const CFE& B = od.b_fe[i];
+    const CFE& C = od.c_fe[i];
+    const double nb = std::hypot(B.re, B.im), ncm = std::hypot(C.re, C.im);
+    RFE t{INFINITY, 0};
+    if (ncm != 0.0) {
+      t.m = tol_ * (nb / ncm) * (nb / ncm);
+      t.e = 2 * (B.e - C.e);
+    }
+    if (rfe_less_host(t, runf)) runf = t;
+    od.sa_min_fe[i] = runf;
+  }
   return 0;
 }
 

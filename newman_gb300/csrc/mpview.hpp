@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "gmp_abi.h"
+#include "view_device.cuh"
 
 namespace nmg {
 
@@ -56,6 +57,15 @@ struct OrbitData {
   std::vector<D2> a, b, c;      // series coefficients A, B, C
   std::vector<double> sa_min;   // prefix minimum of tol |B_i|^2 / |C_i|^2 (index 0 unused)
   bool sa_fp64_ok = true;       // FP64 series terms stay in the normal range
+  // Floatexp copies (FP64 mantissa, int exponent), used when !sa_fp64_ok:
+  std::vector<CFE> a_fe, b_fe, c_fe;
+  std::vector<RFE> sa_min_fe;
+};
+
+// Where the reference orbit starts.
+enum ReferenceMode {
+  REFERENCE_PROBES = 0,  // the reference's probe search (findProbe, mandelbrot.cpp:73-95)
+  REFERENCE_CENTER = 1   // the view center only (one orbit; for deep views)
 };
 
 class MPView {
@@ -95,10 +105,12 @@ class MPView {
   void coordinates(std::vector<D2>& re, std::vector<D2>& im) const;
   // eps = get_d(pt - X[0]) per column / row (mandelbrot.cpp:155-159).
   void eps_tables(const OrbitData& od, std::vector<double>& er, std::vector<double>& ei) const;
+  // The same as floatexp (mantissa and exponent of the truncated value).
+  void eps_tables_fe(std::vector<RFE>& er, std::vector<RFE>& ei) const;
 
   // findProbe + computeSeries (mandelbrot.cpp:73-131), probes on `threads`
-  // host threads.  Fills `out`.
-  int precompute(int threads, OrbitData& out);
+  // host threads (or the view center only, REFERENCE_CENTER).  Fills `out`.
+  int precompute(int threads, OrbitData& out, int reference_mode = REFERENCE_PROBES);
 
   // Box in which every sample lies is provably outside both the main
   // cardioid and the period-2 disk.

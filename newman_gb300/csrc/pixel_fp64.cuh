@@ -171,9 +171,10 @@ NM_HD bool hw_steps(const DeviceView& v, HwState& st, int steps, EscapeValue& ou
 
 // ---- the series front of getIterations (mandelbrot.cpp:144-207) -------------
 struct SeriesFront {
-  C64 eps;       // Y0 - X[0]
-  C64 dfound;    // d[found]
+  C64 eps;       // Y0 - X[0]  (times 2^eps_e)
+  C64 dfound;    // d[found]   (times 2^d_e)
   int32_t dsize; // d.size() after the skip
+  int32_t eps_e, d_e;  // exponents of the floatexp front (0 in the FP64 range)
 };
 
 NM_HD C64 sa_term(const DeviceView& v, int i, C64 eps, C64 eps2, C64 eps3, bool& unstable) {
@@ -283,6 +284,8 @@ NM_HD bool series_front(const DeviceView& v, int r, int c, SeriesFront& f, Escap
   f.eps = eps;
   f.dfound = d;
   f.dsize = dsize;
+  f.eps_e = 0;
+  f.d_e = 0;
   return false;
 }
 
@@ -297,11 +300,19 @@ struct DeltaState {
   int32_t j, i;
 };
 
+NM_HD double scalbn_d(double x, int n) {
+#if defined(__CUDA_ARCH__)
+  return n == 0 ? x : scalbn(x, n);
+#else
+  return n == 0 ? x : std::scalbn(x, n);
+#endif
+}
+
 NM_HD void delta_start(const SeriesFront& f, DeltaState& st) {
-  st.dr = f.dfound.re;
-  st.di = f.dfound.im;
-  st.er = f.eps.re;
-  st.ei = f.eps.im;
+  st.dr = scalbn_d(f.dfound.re, f.d_e);
+  st.di = scalbn_d(f.dfound.im, f.d_e);
+  st.er = scalbn_d(f.eps.re, f.eps_e);
+  st.ei = scalbn_d(f.eps.im, f.eps_e);
   st.j = f.dsize;  // found + 1
   st.i = f.dsize;
 }

@@ -36,7 +36,7 @@ struct FeJob {
   static __device__ __forceinline__ bool init(const DeviceView& v, int r, int c, State& st,
                                               EscapeValue& out, double& sm, bool& und) {
     SeriesFront f;
-    if (series_front(v, r, c, f, out, sm, und)) return true;
+    if (series_front_any(v, r, c, f, out, sm, und)) return true;
     fe_start(f, st);
     return false;
   }
@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(256) fe_front_kernel(DeviceView v, FePassBuffe
       EscapeValue out;
       double sm = 0.0;
       bool und = false;
-      if (series_front(v, r, c, f, out, sm, und)) {
+      if (series_front_any(v, r, c, f, out, sm, und)) {
         store_sample(v, r, c, out, sm);
         finished++;
       } else {

@@ -6,7 +6,7 @@
 // round-to-nearest intrinsics, so no multiply-add is ever contracted.
 #include "engine.hpp"
 #include "persistent.cuh"
-#include "pixel_fp64.cuh"
+#include "pixel_fe64.cuh"
 
 namespace nmg {
 
@@ -39,7 +39,7 @@ struct Delta64Job {
   static __device__ __forceinline__ bool init(const DeviceView& v, int r, int c, State& st,
                                               EscapeValue& out, double& sm, bool& und) {
     SeriesFront f;
-    if (series_front(v, r, c, f, out, sm, und)) return true;
+    if (series_front_any(v, r, c, f, out, sm, und)) return true;
     delta_start(f, st.d);
     return false;
   }

@@ -28,6 +28,16 @@ struct alignas(16) Flt4 {
   float x, y, z, w;
 };
 
+// Floatexp values: FP64 mantissas with an int exponent.
+struct CFE {  // (re + i im) * 2^e
+  double re, im;
+  int32_t e;
+};
+struct RFE {  // m * 2^e
+  double m;
+  int32_t e;
+};
+
 enum CardioidMode : int32_t {
   CARDIOID_PER_SAMPLE = 0,  // evaluate the test for each sample (double-double)
   CARDIOID_NONE = 1,        // the view box is provably outside both regions
@@ -62,7 +72,13 @@ struct DeviceView {
   const Dbl2* sa_c;
   const double* sa_min;    // [xlen] prefix min of tol |B_i|^2/|C_i|^2
   int32_t sa_scan;         // 1: walk the series term by term (no threshold shortcut)
-  int32_t pad_;
+  int32_t sa_fe;           // 1: eps, series and thresholds in floatexp (tables below)
+  const RFE* eps_re_fe;    // [nc]
+  const RFE* eps_im_fe;    // [nr]
+  const CFE* sa_a_fe;      // [xlen]
+  const CFE* sa_b_fe;
+  const CFE* sa_c_fe;
+  const RFE* sa_min_fe;    // [xlen]
 
   EscapeValue* grid;       // [nr*nc]
   double* smooth64;        // optional [nr*nc] unrounded smoothing

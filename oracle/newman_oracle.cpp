@@ -48,7 +48,9 @@ constexpr double kBailout = 1024.0;                 // mandelbrot.cpp:58
 constexpr double kBailout2 = kBailout * kBailout;   // mandelbrot.cpp:59
 constexpr double kMinPreview = 1.5e-16;             // mandelbrot.cpp:257
 
-enum { MODE_REF = 0, MODE_DELTA = 1 };
+// MODE_REF_FE / MODE_DELTA_FE: the same with the floatexp series front, for
+// views whose series terms leave the FP64 range.
+enum { MODE_REF = 0, MODE_DELTA = 1, MODE_REF_FE = 2, MODE_DELTA_FE = 3 };
 
 // RAII holder for one mpf_t at a fixed precision.
 struct MP {
@@ -501,6 +503,179 @@ Pixel get_iterations_delta(View& v, mpf_srcptr y0r, mpf_srcptr y0i, Scratch& s,
   return {v.N, 0.0};
 }
 
+// ---- floatexp series front (views outside the FP64 range) -------------------
+// The reference's series arithmetic on FP64 mantissas with a separate
+// exponent, each result rescaled exactly so that its larger component lies in
+// [0.5, 1).  In the FP64 range it gives the FP64 results; below it, the same
+// operations without overflow (the reference itself turns to NaN there).
+struct FX {
+  double re, im;
+  long e;
+};
+inline FX fx_norm(FX a) {
+  double m = std::max(std::fabs(a.re), std::fabs(a.im));
+  if (m == 0.0) return {a.re, a.im, 0};
+  int k;
+  std::frexp(m, &k);
+  return {std::ldexp(a.re, -k), std::ldexp(a.im, -k), a.e + k};
+}
+inline FX fx_of(mpf_srcptr re, mpf_srcptr im) {
+  long er, ei;
+  double dr = mpf_get_d_2exp(&er, re), di = mpf_get_d_2exp(&ei, im);
+  if (dr == 0.0 && di == 0.0) return {0.0, 0.0, 0};
+  long e = dr == 0.0 ? ei : di == 0.0 ? er : std::max(er, ei);
+  return fx_norm({std::ldexp(dr, (int)(er - e)), std::ldexp(di, (int)(ei - e)), e});
+}
+inline FX fx_mul(FX a, FX b) {
+  LP p = mul({a.re, a.im}, {b.re, b.im});
+  return fx_norm({p.re, p.im, a.e + b.e});
+}
+inline FX fx_sq(FX a) {
+  LP p = sq({a.re, a.im});
+  return fx_norm({p.re, p.im, 2 * a.e});
+}
+inline FX fx_add(FX a, FX b) {
+  if (a.e < b.e) std::swap(a, b);
+  int d = (int)std::max<long>(b.e - a.e, -2000);
+  return fx_norm({a.re + std::ldexp(b.re, d), a.im + std::ldexp(b.im, d), a.e});
+}
+// |a|^2 as (mantissa, exponent)
+inline std::pair<double, long> fx_mag2(FX a) { return {a.re * a.re + a.im * a.im, 2 * a.e}; }
+inline bool fx_less(std::pair<double, long> x, std::pair<double, long> y) {
+  if (!(x.first > 0.0)) return y.first > 0.0;
+  if (!(y.first > 0.0)) return false;
+  int ex, ey;
+  double mx = std::frexp(x.first, &ex), my = std::frexp(y.first, &ey);
+  long tx = ex + x.second, ty = ey + y.second;
+  if (tx != ty) return tx < ty;
+  return mx < my;
+}
+inline double fx_re(FX a) { return std::ldexp(a.re, (int)std::max<long>(a.e, -2000)); }
+inline double fx_im(FX a) { return std::ldexp(a.im, (int)std::max<long>(a.e, -2000)); }
+
+struct SAStateFX {
+  FX eps;
+  size_t dsize;
+  FX dfound;
+};
+
+// series_front with the floatexp series arithmetic (mandelbrot.cpp:144-207).
+bool series_front_fx(View& v, mpf_srcptr y0r, mpf_srcptr y0i, Scratch& s, Pixel& out,
+                     SAStateFX& st) {
+  if (in_cardioid(y0r, y0i, s)) {
+    out = {v.N, 0.0};
+    return true;
+  }
+  mpf_sub(s.yr, y0r, &v.X.re[0]);
+  mpf_sub(s.yi, y0i, &v.X.im[0]);
+  FX eps = fx_of(s.yr, s.yi);
+  FX eps2 = fx_sq(eps);
+  FX eps3 = fx_mul(eps, eps2);
+  const size_t n = v.X.size();
+  auto term = [&](size_t i, bool& unstable) {
+    FX a = fx_mul(fx_of(&v.A.re[i], &v.A.im[i]), eps);
+    FX b = fx_mul(fx_of(&v.B.re[i], &v.B.im[i]), eps2);
+    FX c = fx_mul(fx_of(&v.C.re[i], &v.C.im[i]), eps3);
+    auto bm = fx_mag2(b), cm = fx_mag2(c);
+    bm.first *= v.tol;
+    unstable = fx_less(bm, cm);  // bmag * tol < cmag
+    return fx_add(fx_add(a, b), c);
+  };
+  size_t dsize = n;
+  for (size_t i = 1; i < n; i++) {
+    bool u;
+    term(i, u);
+    if (u) {
+      long good = (long)i - 3;
+      dsize = (size_t)(good < 1 ? 1 : good);
+      break;
+    }
+  }
+  auto dval = [&](size_t k) {
+    if (k == 0) return eps;
+    bool u;
+    return term(k, u);
+  };
+  auto xplusd = [&](size_t k) {
+    FX d = dval(k);
+    mpf_set_d(s.dtmp, fx_re(d));
+    mpf_add(s.yr, &v.X.re[k], s.dtmp);
+    mpf_set_d(s.dtmp, fx_im(d));
+    mpf_add(s.yi, &v.X.im[k], s.dtmp);
+  };
+  size_t found = dsize - 1;
+  xplusd(found);
+  if (bailed_out(s.yr, s.yi)) {
+    long low = 0, high = (long)dsize - 1, mid = (long)dsize / 2;
+    while (low <= high) {
+      xplusd((size_t)mid);
+      if (!bailed_out(s.yr, s.yi))
+        low = mid + 1;
+      else {
+        high = mid - 1;
+        found = (size_t)mid;
+      }
+      mid = (low + high) / 2;
+    }
+    xplusd(found);
+    LP y{mpf_get_d(s.yr), mpf_get_d(s.yi)};
+    out = {(int32_t)found, smoothing_magnitude(sqMag(y))};
+    return true;
+  }
+  st.eps = eps;
+  st.dsize = dsize;
+  st.dfound = dval(found);
+  return false;
+}
+
+// MODE_REF_FE: getIterations with the floatexp series front and the
+// reference's arbitrary-precision continuation.
+Pixel get_iterations_fx(View& v, mpf_srcptr y0r, mpf_srcptr y0i, Scratch& s) {
+  Pixel out;
+  SAStateFX st;
+  if (series_front_fx(v, y0r, y0i, s, out, st)) return out;
+  for (int i = (int)st.dsize; i < v.N; i++) {
+    orbit_step(s.ynr, s.yni, s.yr, s.yi, y0r, y0i, s);
+    if (bailed_out(s.ynr, s.yni)) {
+      LP y{mpf_get_d(s.ynr), mpf_get_d(s.yni)};
+      return {i, smoothing_magnitude(sqMag(y))};
+    }
+    mpf_set(s.yr, s.ynr);
+    mpf_set(s.yi, s.yni);
+  }
+  return {v.N, 0.0};
+}
+
+// MODE_DELTA_FE: the GPU library's FP64 perturbation path on a floatexp view.
+Pixel get_iterations_delta_fx(View& v, mpf_srcptr y0r, mpf_srcptr y0i, Scratch& s,
+                              const std::vector<LP>& Z) {
+  Pixel out;
+  SAStateFX st;
+  if (series_front_fx(v, y0r, y0i, s, out, st)) return out;
+  LP dl{fx_re(st.dfound), fx_im(st.dfound)};
+  const LP eps{fx_re(st.eps), fx_im(st.eps)};
+  size_t j = st.dsize;
+  const size_t zlast = Z.size() - 1;
+  for (int i = (int)st.dsize; i < v.N; i++) {
+    LP z = Z[j];
+    double tr = 2.0 * z.re + dl.re;
+    double ti = 2.0 * z.im + dl.im;
+    double nre = (tr * dl.re - ti * dl.im) + eps.re;
+    double nim = (tr * dl.im + ti * dl.re) + eps.im;
+    dl = {nre, nim};
+    j++;
+    LP y{Z[j].re + dl.re, Z[j].im + dl.im};
+    double r2 = y.re * y.re + y.im * y.im;
+    if (r2 > kBailout2) return {i, smoothing_magnitude(r2)};
+    double d2 = dl.re * dl.re + dl.im * dl.im;
+    if (r2 < d2 || j == zlast) {
+      dl = y;
+      j = 0;
+    }
+  }
+  return {v.N, 0.0};
+}
+
 // The FP64 copy of the orbit the delta path iterates against.
 std::vector<LP> delta_orbit(View& v) {
   std::vector<LP> Z;
@@ -636,6 +811,22 @@ int nmo_precompute(nmo_view* h, int threads) {
   return 0;
 }
 
+// precompute with the view center as the only probe (pointAt(nr/2 - 1, nc/2)
+// is exactly the center): the reference orbit of the library's
+// REFERENCE_CENTER mode.
+int nmo_precompute_center(nmo_view* h) {
+  View* v = reinterpret_cast<View*>(h);
+  v->X.clear(); v->A.clear(); v->B.clear(); v->C.clear();
+  MP pr(v->bits), pi(v->bits), tmp(v->bits);
+  v->point_re(v->nc / 2, pr, tmp);
+  v->point_im(v->nr / 2 - 1, pi, tmp);
+  compute_orbit(*v, pr, pi, v->X);
+  compute_series(*v);
+  v->probe_index = 0;
+  v->precomputed = true;
+  return 0;
+}
+
 int nmo_probe_index(nmo_view* h) { return reinterpret_cast<View*>(h)->probe_index; }
 int nmo_orbit_length(nmo_view* h) { return (int)reinterpret_cast<View*>(h)->X.size(); }
 
@@ -672,9 +863,9 @@ int nmo_render_pixels(nmo_view* h, int mode, long npix, const int32_t* rows, con
   View* v = reinterpret_cast<View*>(h);
   const bool hw = v->use_hardware();
   if (!hw && !v->precomputed) return 3;
-  if (mode == MODE_DELTA && hw) return 4;
+  if (mode != MODE_REF && hw) return 4;
   std::vector<LP> Z;
-  if (mode == MODE_DELTA) Z = delta_orbit(*v);
+  if (mode == MODE_DELTA || mode == MODE_DELTA_FE) Z = delta_orbit(*v);
   for (long k = 0; k < npix; k++)
     if (rows[k] < 0 || rows[k] >= v->nr || cols[k] < 0 || cols[k] >= v->nc) return 5;
   parallel_for((size_t)npix, threads, [&](size_t k) {
@@ -687,7 +878,9 @@ int nmo_render_pixels(nmo_view* h, int mode, long npix, const int32_t* rows, con
     Pixel p;
     if (hw) p = get_iterations_hw(*v, pr, pi, *s);
     else if (mode == MODE_REF) p = get_iterations(*v, pr, pi, *s);
-    else p = get_iterations_delta(*v, pr, pi, *s, Z);
+    else if (mode == MODE_DELTA) p = get_iterations_delta(*v, pr, pi, *s, Z);
+    else if (mode == MODE_REF_FE) p = get_iterations_fx(*v, pr, pi, *s);
+    else p = get_iterations_delta_fx(*v, pr, pi, *s, Z);
     iters[k] = p.iterations;
     smooth[k] = p.smoothing;
   });

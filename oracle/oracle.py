@@ -13,6 +13,8 @@ from . import build as _build
 
 MODE_REF = 0
 MODE_DELTA = 1
+MODE_REF_FE = 2
+MODE_DELTA_FE = 3
 
 _lib = None
 
@@ -35,6 +37,7 @@ def lib():
         L.nmo_scale_up.argtypes = [vp, i32]
         L.nmo_scale_down.argtypes = [vp, i32]
         L.nmo_precompute.argtypes = [vp, i32]
+        L.nmo_precompute_center.argtypes = [vp]
         L.nmo_export_orbit.argtypes = [vp] + [P(dbl)] * 5
         L.nmo_coords.argtypes = [vp, P(dbl), P(dbl)]
         L.nmo_render_pixels.argtypes = [vp, i32, ctypes.c_long, P(ctypes.c_int32),
@@ -95,8 +98,11 @@ class OracleView:
     def scale_down(self, sc):
         assert lib().nmo_scale_down(self._h, sc) == 0
 
-    def precompute(self, threads=None):
-        assert lib().nmo_precompute(self._h, threads or default_threads()) == 0
+    def precompute(self, threads=None, center=False):
+        if center:
+            assert lib().nmo_precompute_center(self._h) == 0
+        else:
+            assert lib().nmo_precompute(self._h, threads or default_threads()) == 0
 
     def export_orbit(self):
         n = self.orbit_length

@@ -46,7 +46,9 @@ def render_gpu(cre, cim, step, n):
     import newman_gb300 as nm
     m = nm.Mandelbrot(GRID, GRID)
     m.set_view(cre, cim, step, step, n)
-    m.set_path(nm.PATH_FP64)
+    # the reference's choice: its double loop while useHardware(), else FP64
+    # perturbation -- what MODE_REF / MODE_DELTA_FE compute on the CPU
+    m.set_path(nm.PATH_REFERENCE)
     m.set_option(nm.OPT_REFERENCE, nm.REFERENCE_CENTER)
     m.precompute()
     m.render()

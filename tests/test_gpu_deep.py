@@ -48,10 +48,10 @@ def gpu_render(nm, cre, cim, step, grid, N, path):
     return m
 
 
-@pytest.mark.parametrize("k", [5, 9])
+@pytest.mark.parametrize("k", [9, 30, 72])
 def test_deep_fp64_matches_oracle(nm, oracle_mod, k):
     cre, cim, step = view_at(k, 64)
-    N = 100000
+    N = 300000
     m = gpu_render(nm, cre, cim, step, 64, N, nm.PATH_FP64)
     o = oracle_mod.OracleView(64, 64)
     o.set_view(cre, cim, step, step, N)
@@ -62,14 +62,14 @@ def test_deep_fp64_matches_oracle(nm, oracle_mod, k):
     g = m.grid()["iterations"][rows.ravel(), cols.ravel()]
     assert np.array_equal(g, it)
     assert np.abs(m.smoothing64()[rows.ravel(), cols.ravel()] - sm).max() <= 1e-12
-    mp_it, _ = o.render_pixels(rows.ravel()[:60], cols.ravel()[:60], oracle_mod.MODE_REF_FE)
-    assert (mp_it == it[:60]).mean() >= 0.9
+    mp_it, _ = o.render_pixels(rows.ravel()[:24], cols.ravel()[:24], oracle_mod.MODE_REF_FE)
+    assert (mp_it == it[:24]).mean() >= 0.75
 
 
-@pytest.mark.parametrize("k", [5, 9])
+@pytest.mark.parametrize("k", [9, 30, 72])
 def test_deep_fe32_matches_fp64(nm, k):
     cre, cim, step = view_at(k, 256)
-    N = 100000
+    N = 300000
     a = gpu_render(nm, cre, cim, step, 256, N, nm.PATH_FP64)
     b = gpu_render(nm, cre, cim, step, 256, N, nm.PATH_FE32)
     same = (a.grid()["iterations"] == b.grid()["iterations"]).mean()

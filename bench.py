@@ -333,6 +333,106 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def video_views(nframes, nr, nc, w0="4.0", w1="1e-200", n0=1000, n1=500000):
+    """Frames of the batched zoom video: widths geometric from w0 to w1, N
+    linear from n0 to n1, into the C2 center."""
+    from decimal import Decimal, getcontext
+    getcontext().prec = 60
+    a, b = Decimal(w0), Decimal(w1)
+    out = []
+    for k in range(nframes):
+        t = Decimal(k) / Decimal(max(1, nframes - 1))
+        out.append((str((a * (b / a) ** t) / nc), int(round(n0 + (n1 - n0) * float(t)))))
+    return out
+
+
+def run_video(args):
+    """240 frames of 1280x720 with 2x2 samples (widths 4 -> 1e-200, N 1e3 ->
+    5e5): all frames in one batched CUDA-graph launch (FE32 below the double
+    path's range) against frame-at-a-time plain FP64."""
+    import concurrent.futures as cf
+    import torch
+    import newman_gb300 as nm
+    torch.cuda.set_device(0)
+    nf, nr, nc, sc = args.frames, 720, 1280, 2
+    views = video_views(nf, nr, nc)
+
+    def frame(step, N, deep_path):
+        m = nm.Mandelbrot(nr, nc)
+        m.set_view(CENTER[0], CENTER[1], step, step, N, TOL)
+        m.scaleUp(sc)
+        if not m.useHardware():
+            m.set_path(deep_path)
+            m.set_option(nm.OPT_REFERENCE, nm.REFERENCE_CENTER)
+        m.precompute()
+        return m
+
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 8) as ex:
+        fe_frames = list(ex.map(lambda v: frame(v[0], v[1], nm.PATH_FE32), views))
+    precompute_s = time.perf_counter() - t0
+    batch = nm.Batch(sc=sc)
+    for f in fe_frames:
+        batch.add(f)
+    tuned = None
+    if args.autotune:
+        tuned = batch.autotune(stride=max(1, nf // 10))
+    for _ in range(args.warmup):
+        batch.render()
+    times = []
+    with ClockSampler(0) as clocks:
+        for _ in range(args.steps):
+            batch.render()
+            times.append(batch.stat(nm.STAT_KERNEL_NS) * 1e-6)
+    ms = float(np.mean(times))
+    executed = batch.stat(nm.STAT_EXECUTED_ITERS)
+    rework = batch.stat(nm.STAT_FP64_REWORK)
+    out = batch.frames_out()
+    eff = int(sum(int(f.grid()["iterations"].astype(np.int64).sum()) for f in fe_frames))
+
+    # frame at a time, plain FP64 (the reference's double path where it applies)
+    fp_frames = [f.copy() for f in fe_frames]
+    fp_ms = 0.0
+    for f in fp_frames:
+        if not f.useHardware():
+            f.set_path(nm.PATH_FP64)
+        f.upload()
+        f.render()  # warm
+        f.render()
+        fp_ms += f.stat(nm.STAT_KERNEL_NS) * 1e-6
+    same = total = 0
+    for a, b in zip(fe_frames, fp_frames):
+        ga, gb = a.grid()["iterations"], b.grid()["iterations"]
+        same += int((ga == gb).sum())
+        total += ga.size
+    # e2e: one graph launch plus the reduced frames to host
+    e2e = []
+    for _ in range(2):
+        t1 = time.perf_counter()
+        batch.render()
+        batch.frames_out()
+        e2e.append(time.perf_counter() - t1)
+    line = {
+        "metric": "frames/s, %d-frame zoom video (1280x720, 2x2 samples, widths 4 -> 1e-200)" % nf,
+        "value": nf / (ms * 1e-3), "unit": "frames/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32 float-float + int exponent (deep frames)",
+        "data": "synthetic views (no dataset)",
+        "config": {"workload": "newman C4 batched zoom video", "frames": nf, "rows": nr,
+                   "cols": nc, "multisample": sc, "widths": ["4.0", "1e-200"],
+                   "max_iter": [1000, 500000], "autotuned": tuned},
+        "frame_at_a_time_fp64": {"ms": fp_ms, "value": nf / (fp_ms * 1e-3), "unit": "frames/s"},
+        "speedup_vs_fp64_frame_at_a_time": fp_ms / ms,
+        "exact_iter_fraction_vs_fp64": same / total, "fp64_rework_samples": rework,
+        "executed_iters_per_step": executed, "effective_iters_per_step": eff,
+        "pixel_iters_per_s": eff / (ms * 1e-3), "precompute_s": precompute_s,
+        "clocks": clocks.summary(),
+        "e2e": {"value": nf / float(np.mean(e2e)), "unit": "frames/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": sum(o.nbytes for o in out)},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -344,9 +444,14 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile", type=int, default=0,
                     help="render each path once on a 1/DIV-size crop and exit (ncu case)")
+    ap.add_argument("--workload", default="c2", choices=["c2", "video"])
+    ap.add_argument("--frames", type=int, default=240)
+    ap.add_argument("--autotune", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "video":
+        run_video(args)
     else:
         run_ours(args)
 

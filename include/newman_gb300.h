@@ -63,8 +63,9 @@ enum nm_option {
   NM_OPT_BLOCKS = 5,      /* persistent blocks (0 = fill the GPU) */
   NM_OPT_RENORM = 6,      /* FE32: steps between exponent renormalisations */
   NM_OPT_FE32_SINGLE_PASS = 7, /* FE32 in one persistent kernel (default: three passes) */
-  NM_OPT_REFERENCE = 8    /* reference orbit: 0 the reference's probe search
+  NM_OPT_REFERENCE = 8,   /* reference orbit: 0 the reference's probe search
                              (findProbe, mandelbrot.cpp:73-95), 1 the view center */
+  NM_OPT_BATCH_GRAPH = 9  /* batches: 1 replay one captured CUDA graph (default), 0 launch */
 };
 
 enum nm_stat {
@@ -152,6 +153,30 @@ int nm_zoom(nm_handle* h, float scale);                            /* mandelbrot
 int nm_zoom_at(nm_handle* h, float scale, int r, int c, int sc);   /* mandelbrot.cpp:304-316 */
 int nm_load_legacy(nm_handle* h, const char* path);                /* mandelbrot.cpp:19-35 */
 int nm_save(const nm_handle* h, const char* path);                 /* viewer.cpp:12-23 */
+
+/* Batches: many frames rendered together, e.g. every frame of a zoom video,
+   each frame a handle with its own view, orbit, series skip and N (no
+   reference counterpart; the reference renders one view at a time).  The
+   first nm_batch_render captures all of the batch's kernels -- the FE32
+   passes over every FE32 frame at once, the double-path and FP64 frames, and
+   the multisample reduce of every frame -- into one CUDA graph, and every
+   render replays it.  Frames must be precomputed first and stay alive while
+   in the batch; a frame whose tables or grid change is noticed and the graph
+   rebuilt.  sc: the frames' multisample factor (their rows and columns are
+   multiples of it); nm_batch_frames returns the reduced frames, frame-major. */
+typedef struct nm_batch nm_batch;
+nm_batch* nm_batch_create(int sc);
+void nm_batch_destroy(nm_batch* b);
+int nm_batch_add(nm_batch* b, nm_handle* frame);
+/* NM_OPT_TILE_W, NM_OPT_TILE_H, NM_OPT_CHUNK, NM_OPT_RENORM, NM_OPT_BATCH_GRAPH */
+int nm_batch_set_option(nm_batch* b, int option, long long value);
+int nm_batch_render(nm_batch* b);
+/* NM_STAT_EXECUTED_ITERS, NM_STAT_SAMPLES, NM_STAT_FP64_REWORK, NM_STAT_KERNEL_NS */
+int nm_batch_get_stat(nm_batch* b, int stat, long long* value);
+int nm_batch_frames(nm_batch* b, nm_escape_value* host_out);
+/* Times every tile shape (8x8 .. 64x64) and FE32 renormalisation interval
+   (8 .. 256) on every stride-th frame and keeps the fastest. */
+int nm_batch_autotune(nm_batch* b, int stride, int* tile_w, int* tile_h, int* renorm);
 
 /* Render the handle's view on the FP32-floatexp path into device memory the
    caller owns, allocating nothing (no cudaMalloc, cudaFree or allocating

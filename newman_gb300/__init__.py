@@ -20,7 +20,7 @@ NM_OK, NM_ERR_ARG, NM_ERR_PARSE, NM_ERR_STATE, NM_ERR_CUDA, NM_ERR_CANCELLED, NM
     NM_ERR_UNSUPPORTED = range(8)
 PATH_REFERENCE, PATH_FP64, PATH_FE32 = 0, 1, 2
 OPT_TILE_W, OPT_TILE_H, OPT_CHUNK, OPT_KEEP_SMOOTH64, OPT_THREADS, OPT_BLOCKS, OPT_RENORM, \
-    OPT_FE32_SINGLE_PASS, OPT_REFERENCE = range(9)
+    OPT_FE32_SINGLE_PASS, OPT_REFERENCE, OPT_BATCH_GRAPH = range(10)
 REFERENCE_PROBES, REFERENCE_CENTER = 0, 1
 STAT_CARDIOID_UNDECIDED, STAT_EXECUTED_ITERS, STAT_SAMPLES, STAT_REBASES, STAT_FP64_REWORK = range(5)
 STAT_ORBIT_LENGTH, STAT_PROBE_INDEX, STAT_PRECISION_BITS, STAT_PRECOMPUTE_US = 16, 17, 18, 19
@@ -37,6 +37,8 @@ EXPORTS = (
     "nm_at", "nm_at_sc", "nm_scale_up", "nm_scale_down", "nm_reduce", "nm_get_grid",
     "nm_get_smoothing64", "nm_device_grid", "nm_point_at", "nm_translate", "nm_zoom",
     "nm_zoom_at", "nm_load_legacy", "nm_save", "nm_peak_flops", "nm_render_fe32_noalloc",
+    "nm_batch_create", "nm_batch_destroy", "nm_batch_add", "nm_batch_set_option",
+    "nm_batch_render", "nm_batch_get_stat", "nm_batch_frames", "nm_batch_autotune",
 )
 
 
@@ -104,6 +106,14 @@ def load_library(path=LIB_PATH):
         "nm_save": (i32, [vp, cp]),
         "nm_peak_flops": (i32, [i32, P(dbl)]),
         "nm_render_fe32_noalloc": (i32, [vp, vp, vp]),
+        "nm_batch_create": (vp, [i32]),
+        "nm_batch_destroy": (None, [vp]),
+        "nm_batch_add": (i32, [vp, vp]),
+        "nm_batch_set_option": (i32, [vp, i32, ll]),
+        "nm_batch_render": (i32, [vp]),
+        "nm_batch_get_stat": (i32, [vp, i32, P(ll)]),
+        "nm_batch_frames": (i32, [vp, vp]),
+        "nm_batch_autotune": (i32, [vp, i32, P(i32), P(i32), P(i32)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -120,6 +130,56 @@ def _check(rc):
 
 def _s(x):
     return str(x).encode()
+
+
+class Batch:
+    """Frames rendered together by one CUDA graph (nm_batch_*).  Keeps the
+    Mandelbrot objects it was given alive."""
+
+    def __init__(self, sc=1):
+        L = load_library()
+        self._b = L.nm_batch_create(int(sc))
+        if not self._b:
+            raise NewmanError(NM_ERR_ARG, L.nm_last_error().decode())
+        self.sc = int(sc)
+        self.frames = []
+
+    def __del__(self):
+        b, self._b = getattr(self, "_b", None), None
+        if b and _lib is not None:
+            _lib.nm_batch_destroy(b)
+
+    def add(self, frame):
+        _check(_lib.nm_batch_add(self._b, frame._h))
+        self.frames.append(frame)
+
+    def set_option(self, option, value):
+        _check(_lib.nm_batch_set_option(self._b, int(option), int(value)))
+
+    def render(self):
+        _check(_lib.nm_batch_render(self._b))
+
+    def stat(self, which):
+        v = ctypes.c_longlong(0)
+        _check(_lib.nm_batch_get_stat(self._b, int(which), ctypes.byref(v)))
+        return v.value
+
+    def frames_out(self):
+        """The reduced frames as a list of (rows/sc, cols/sc) structured arrays."""
+        shapes = [(f.rows() // self.sc, f.cols() // self.sc) for f in self.frames]
+        flat = np.empty(sum(r * c for r, c in shapes), ESCAPE_DTYPE)
+        _check(_lib.nm_batch_frames(self._b, flat.ctypes.data))
+        out, at = [], 0
+        for r, c in shapes:
+            out.append(flat[at:at + r * c].reshape(r, c))
+            at += r * c
+        return out
+
+    def autotune(self, stride=1):
+        w, h, rn = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _check(_lib.nm_batch_autotune(self._b, int(stride), ctypes.byref(w), ctypes.byref(h),
+                                      ctypes.byref(rn)))
+        return w.value, h.value, rn.value
 
 
 def peak_flops(kind):

@@ -17,16 +17,23 @@
 #include <vector>
 
 #include "engine.hpp"
+#include "handle.hpp"
 #include "mpview.hpp"
 
 using nmg::Dbl2;
 using nmg::EscapeValue;
 
+using nmg::DevBuf;
+using nmg::fail;
+using namespace nmg::scratch;
+
 namespace {
 
 thread_local std::string g_last_error;
 
-int fail(int code, const char* fmt, ...) {
+}  // namespace
+
+int nmg::fail(int code, const char* fmt, ...) {
   char buf[512];
   va_list ap;
   va_start(ap, fmt);
@@ -35,111 +42,6 @@ int fail(int code, const char* fmt, ...) {
   g_last_error = buf;
   return code;
 }
-
-#define NM_CUDA(call)                                                                  \
-  do {                                                                                 \
-    cudaError_t e_ = (call);                                                           \
-    if (e_ != cudaSuccess)                                                             \
-      return fail(NM_ERR_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
-                  __LINE__);                                                           \
-  } while (0)
-
-// Device buffer that grows on demand.
-template <typename T>
-struct DevBuf {
-  T* p = nullptr;
-  size_t n = 0;
-  DevBuf() = default;
-  DevBuf(const DevBuf&) = delete;
-  DevBuf& operator=(const DevBuf&) = delete;
-  ~DevBuf() { release(); }
-  void release() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    n = 0;
-  }
-  cudaError_t reserve(size_t count) {
-    if (count <= n && p) return cudaSuccess;
-    release();
-    cudaError_t e = cudaMalloc(&p, (count ? count : 1) * sizeof(T));
-    if (e == cudaSuccess) n = count;
-    return e;
-  }
-};
-
-static_assert(sizeof(nm_escape_value) == sizeof(EscapeValue), "grid layout");
-
-// Device scratch words of a handle: the persistent kernels' work counters and
-// statistics, and the length of the FE32 rework list.
-constexpr int kNextMain = 0;
-constexpr int kStatsMain = 1;
-constexpr int kNextRework = kStatsMain + nmg::STAT_COUNT;
-constexpr int kStatsRework = kNextRework + 1;
-constexpr int kReworkCount = kStatsRework + nmg::STAT_COUNT;
-constexpr int kWorkCount = kReworkCount + 1;  // FE32 pass pipeline: samples to iterate
-constexpr int kScratchWords = kWorkCount + 1;
-
-}  // namespace
-
-struct nm_handle {
-  nmg::MPView view;
-  int device = 0;
-  int path = NM_PATH_REFERENCE;
-  int tile_w = 16, tile_h = 16, chunk = 32, blocks = 0, threads = 0, renorm = 32;
-  bool keep_smooth64 = false;
-  cudaStream_t stream = nullptr;
-
-  // grid
-  DevBuf<EscapeValue> grid;
-  DevBuf<double> smooth64;
-  int grid_nr = 0, grid_nc = 0;
-
-  // per-view tables
-  std::vector<Dbl2> coord_re, coord_im;
-  std::vector<double> eps_re, eps_im;
-  nmg::OrbitData od;
-  bool precomputed = false;   // od + eps valid for the current view
-  bool coords_valid = false;  // coord tables valid for the current view
-  bool uploaded = false;      // device copies current
-  bool outside_cardioid = false;
-  double precompute_us = 0.0;
-  DevBuf<Dbl2> d_coord_re, d_coord_im, d_z, d_xhi, d_xlo, d_a, d_b, d_c;
-  DevBuf<nmg::Flt4> d_zf;
-  DevBuf<double> d_eps_re, d_eps_im, d_sa_min;
-  // floatexp tables (views outside the FP64 range)
-  std::vector<nmg::RFE> eps_re_fe, eps_im_fe;
-  DevBuf<nmg::RFE> d_eps_re_fe, d_eps_im_fe, d_sa_min_fe;
-  DevBuf<nmg::CFE> d_a_fe, d_b_fe, d_c_fe;
-  int reference_mode = nmg::REFERENCE_PROBES;
-
-  // scratch: work counters, statistics, and the FE32 rework list
-  DevBuf<unsigned long long> d_scratch;  // kScratchWords, layout below
-  DevBuf<unsigned int> d_rework;
-  int* cancel_host = nullptr;
-  int* cancel_dev = nullptr;
-  long long expected_samples = 0;
-  // events around the last render's kernels: [0] before, [1] after the main
-  // kernel (or FE32 passes), [2] after the FE32 rework kernel, [3]/[4] around
-  // the FE32 iteration pass
-  cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
-  bool timed_rework = false, timed_iter = false;
-  bool fe_single_pass = false;  // FE32 in one persistent kernel instead of the passes
-  DevBuf<char> d_fe_state, d_fe_result;
-  DevBuf<unsigned int> d_work;
-
-  nm_handle(int nr, int nc) : view(nr, nc) {}
-  ~nm_handle() {
-    for (cudaEvent_t e : ev)
-      if (e) cudaEventDestroy(e);
-    if (stream) cudaStreamDestroy(stream);
-    if (cancel_host) cudaFreeHost(cancel_host);
-  }
-  void invalidate() {
-    precomputed = false;
-    coords_valid = false;
-    uploaded = false;
-  }
-};
 
 namespace {
 
@@ -261,6 +163,55 @@ void set_fe_tables(const nm_handle* h, nmg::DeviceView& v) {
 }
 
 }  // namespace
+
+int nmg::prepare_view(nm_handle* h, int r0, int r1, nmg::DeviceView& v, nmg::KernelKind& kind) {
+  const int nr = h->view.rows(), nc = h->view.cols();
+  const bool hw = h->view.use_hardware() && h->path == NM_PATH_REFERENCE;
+  if (!hw && !h->precomputed)
+    return fail(NM_ERR_STATE, "deep view: nm_precompute must run before rendering");
+  if (int rc = ensure_grid(h)) return rc;
+  if (int rc = ensure_coords(h)) return rc;
+  if (!h->uploaded)
+    if (int rc = do_upload(h)) return rc;
+  std::memset(&v, 0, sizeof v);
+  v.nr = nr;
+  v.nc = nc;
+  v.N = h->view.iterations();
+  v.cardioid_mode = h->outside_cardioid ? nmg::CARDIOID_NONE : nmg::CARDIOID_PER_SAMPLE;
+  v.tol = h->view.tolerance();
+  v.bailout2 = 1024.0 * 1024.0;
+  v.log_bailout = std::log(1024.0);
+  v.tile_w = h->tile_w;
+  v.tile_h = h->tile_h;
+  v.row0 = r0;
+  v.row1 = r1;
+  v.tiles_x = (nc + h->tile_w - 1) / h->tile_w;
+  v.tiles_y = (r1 - r0 + h->tile_h - 1) / h->tile_h;
+  v.total = (long long)v.tiles_x * v.tiles_y * h->tile_w * h->tile_h;
+  v.coord_re = h->d_coord_re.p;
+  v.coord_im = h->d_coord_im.p;
+  if (!hw) {
+    v.eps_re = h->d_eps_re.p;
+    v.eps_im = h->d_eps_im.p;
+    v.z = h->d_z.p;
+    v.zf = h->d_zf.p;
+    v.zlen = (int)h->od.z.size();
+    v.xlen = h->od.xlen;
+    v.xhi = h->d_xhi.p;
+    v.xlo = h->d_xlo.p;
+    v.sa_a = h->d_a.p;
+    v.sa_b = h->d_b.p;
+    v.sa_c = h->d_c.p;
+    v.sa_min = h->d_sa_min.p;
+    set_fe_tables(h, v);
+  }
+  v.grid = h->grid.p;
+  v.smooth64 = h->keep_smooth64 ? h->smooth64.p : nullptr;
+  kind = hw ? nmg::KERNEL_HW : (h->path == NM_PATH_FE32 ? nmg::KERNEL_FE32 : nmg::KERNEL_DELTA64);
+  return NM_OK;
+}
+
+
 
 extern "C" {
 
@@ -486,53 +437,10 @@ int nm_render_rows(nm_handle* h, int r0, int r1, void* stream_arg) {
   if (int rc = check_handle(h)) return rc;
   const int nr = h->view.rows(), nc = h->view.cols();
   if (r0 < 0 || r1 > nr || r0 > r1) return fail(NM_ERR_ARG, "rows [%d, %d) of %d", r0, r1, nr);
-  const bool hw = h->view.use_hardware() && h->path == NM_PATH_REFERENCE;
-  if (!hw && !h->precomputed)
-    return fail(NM_ERR_STATE, "deep view: nm_precompute must run before rendering");
-  if (int rc = ensure_grid(h)) return rc;
-  if (int rc = ensure_coords(h)) return rc;
-  if (!h->uploaded)
-    if (int rc = do_upload(h)) return rc;
-  cudaStream_t s = stream_arg ? (cudaStream_t)stream_arg : h->stream;
-
   nmg::DeviceView v;
-  std::memset(&v, 0, sizeof v);
-  v.nr = nr;
-  v.nc = nc;
-  v.N = h->view.iterations();
-  v.cardioid_mode = h->outside_cardioid ? nmg::CARDIOID_NONE : nmg::CARDIOID_PER_SAMPLE;
-  v.tol = h->view.tolerance();
-  v.bailout2 = 1024.0 * 1024.0;
-  v.log_bailout = std::log(1024.0);
-  v.tile_w = h->tile_w;
-  v.tile_h = h->tile_h;
-  v.row0 = r0;
-  v.row1 = r1;
-  v.tiles_x = (nc + h->tile_w - 1) / h->tile_w;
-  v.tiles_y = (r1 - r0 + h->tile_h - 1) / h->tile_h;
-  v.total = (long long)v.tiles_x * v.tiles_y * h->tile_w * h->tile_h;
-  v.coord_re = h->d_coord_re.p;
-  v.coord_im = h->d_coord_im.p;
-  if (!hw) {
-    v.eps_re = h->d_eps_re.p;
-    v.eps_im = h->d_eps_im.p;
-    v.z = h->d_z.p;
-    v.zf = h->d_zf.p;
-    v.zlen = (int)h->od.z.size();
-    v.xlen = h->od.xlen;
-    v.xhi = h->d_xhi.p;
-    v.xlo = h->d_xlo.p;
-    v.sa_a = h->d_a.p;
-    v.sa_b = h->d_b.p;
-    v.sa_c = h->d_c.p;
-    v.sa_min = h->d_sa_min.p;
-    set_fe_tables(h, v);
-  }
-  v.grid = h->grid.p;
-  v.smooth64 = h->keep_smooth64 ? h->smooth64.p : nullptr;
-
-  nmg::KernelKind kind = hw ? nmg::KERNEL_HW
-                       : (h->path == NM_PATH_FE32 ? nmg::KERNEL_FE32 : nmg::KERNEL_DELTA64);
+  nmg::KernelKind kind;
+  if (int rc = prepare_view(h, r0, r1, v, kind)) return rc;
+  cudaStream_t s = stream_arg ? (cudaStream_t)stream_arg : h->stream;
   nmg::RenderCtl ctl;
   std::memset(&ctl, 0, sizeof ctl);
   ctl.next = h->d_scratch.p + kNextMain;

@@ -54,6 +54,36 @@ cudaError_t launch_fe32_passes(const DeviceView& v, const FePassBuffers& b, cons
                                cudaStream_t stream, int device, int blocks, int chunk,
                                cudaEvent_t iter_begin, cudaEvent_t iter_end);
 
+// ---- batches of frames (render_batch.cu) ------------------------------------
+// Frames rendered by one kernel: global sample index g of frame f runs over
+// [offsets[f], offsets[f+1]).
+struct BatchGroup {
+  const DeviceView* views;   // [n], device memory
+  const long long* offsets;  // [n+1], device memory
+  int n;
+  long long total;
+};
+// One frame's multisample mean: (nr*sc x nc*sc) samples -> nr x nc pixels at
+// out; its pixels are [offset, offset + nr*nc) of the batch's output.
+struct ReduceJob {
+  const EscapeValue* in;
+  EscapeValue* out;
+  int nc, sc;
+  long long offset;
+};
+struct BatchLaunch {
+  int device;
+  BatchGroup fe, hw, fp64;
+  FePassBuffers fe_buf;
+  RenderCtl fe_ctl, rework_ctl, hw_ctl, fp64_ctl;
+  int fe_chunk, chunk;
+  const ReduceJob* reduce;  // [nreduce], device memory
+  int nreduce;
+  long long reduce_total;
+};
+// Every launch of one batch render, in stream order (capturable).
+cudaError_t launch_batch(const BatchLaunch& launch, cudaStream_t stream);
+
 // Persistent, warp-refilled launches: every warp keeps its 32 lanes busy by
 // pulling new samples from `ctl.next` as lanes finish.
 cudaError_t launch_render(KernelKind kind, const DeviceView& v, const RenderCtl& ctl,

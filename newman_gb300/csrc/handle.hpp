@@ -1,0 +1,138 @@
+// Internal declarations shared by the C ABI's translation units (capi.cpp,
+// batch.cpp): the handle behind nm_handle, device buffers, error reporting.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <string>
+#include <vector>
+
+#include "engine.hpp"
+#include "mpview.hpp"
+#include "newman_gb300.h"
+
+namespace nmg {
+
+// Records the message of the failing call (nm_last_error) and returns code.
+int fail(int code, const char* fmt, ...);
+
+
+#define NM_CUDA(call)                                                                  \
+  do {                                                                                 \
+    cudaError_t e_ = (call);                                                           \
+    if (e_ != cudaSuccess)                                                             \
+      return fail(NM_ERR_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
+                  __LINE__);                                                           \
+  } while (0)
+
+// Device buffer that grows on demand.
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  cudaError_t reserve(size_t count) {
+    if (count <= n && p) return cudaSuccess;
+    release();
+    cudaError_t e = cudaMalloc(&p, (count ? count : 1) * sizeof(T));
+    if (e == cudaSuccess) n = count;
+    return e;
+  }
+};
+
+static_assert(sizeof(nm_escape_value) == sizeof(EscapeValue), "grid layout");
+
+// Device scratch words of a handle: the persistent kernels' work counters and
+// statistics, and the length of the FE32 rework list.
+namespace scratch {
+constexpr int kNextMain = 0;
+constexpr int kStatsMain = 1;
+constexpr int kNextRework = kStatsMain + nmg::STAT_COUNT;
+constexpr int kStatsRework = kNextRework + 1;
+constexpr int kReworkCount = kStatsRework + nmg::STAT_COUNT;
+constexpr int kWorkCount = kReworkCount + 1;  // FE32 pass pipeline: samples to iterate
+constexpr int kScratchWords = kWorkCount + 1;
+}  // namespace scratch
+
+}  // namespace nmg
+
+struct nm_handle {
+  template <typename T>
+  using DevBuf = nmg::DevBuf<T>;
+  using EscapeValue = nmg::EscapeValue;
+  using Dbl2 = nmg::Dbl2;
+  nmg::MPView view;
+  int device = 0;
+  int path = NM_PATH_REFERENCE;
+  int tile_w = 16, tile_h = 16, chunk = 32, blocks = 0, threads = 0, renorm = 32;
+  bool keep_smooth64 = false;
+  cudaStream_t stream = nullptr;
+
+  // grid
+  DevBuf<EscapeValue> grid;
+  DevBuf<double> smooth64;
+  int grid_nr = 0, grid_nc = 0;
+
+  // per-view tables
+  std::vector<Dbl2> coord_re, coord_im;
+  std::vector<double> eps_re, eps_im;
+  nmg::OrbitData od;
+  bool precomputed = false;   // od + eps valid for the current view
+  bool coords_valid = false;  // coord tables valid for the current view
+  bool uploaded = false;      // device copies current
+  bool outside_cardioid = false;
+  double precompute_us = 0.0;
+  DevBuf<Dbl2> d_coord_re, d_coord_im, d_z, d_xhi, d_xlo, d_a, d_b, d_c;
+  DevBuf<nmg::Flt4> d_zf;
+  DevBuf<double> d_eps_re, d_eps_im, d_sa_min;
+  // floatexp tables (views outside the FP64 range)
+  std::vector<nmg::RFE> eps_re_fe, eps_im_fe;
+  DevBuf<nmg::RFE> d_eps_re_fe, d_eps_im_fe, d_sa_min_fe;
+  DevBuf<nmg::CFE> d_a_fe, d_b_fe, d_c_fe;
+  int reference_mode = nmg::REFERENCE_PROBES;
+
+  // scratch: work counters, statistics, and the FE32 rework list
+  DevBuf<unsigned long long> d_scratch;  // kScratchWords, layout below
+  DevBuf<unsigned int> d_rework;
+  int* cancel_host = nullptr;
+  int* cancel_dev = nullptr;
+  long long expected_samples = 0;
+  // events around the last render's kernels: [0] before, [1] after the main
+  // kernel (or FE32 passes), [2] after the FE32 rework kernel, [3]/[4] around
+  // the FE32 iteration pass
+  cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  bool timed_rework = false, timed_iter = false;
+  bool fe_single_pass = false;  // FE32 in one persistent kernel instead of the passes
+  DevBuf<char> d_fe_state, d_fe_result;
+  DevBuf<unsigned int> d_work;
+
+  nm_handle(int nr, int nc) : view(nr, nc) {}
+  ~nm_handle() {
+    for (cudaEvent_t e : ev)
+      if (e) cudaEventDestroy(e);
+    if (stream) cudaStreamDestroy(stream);
+    if (cancel_host) cudaFreeHost(cancel_host);
+  }
+  void invalidate() {
+    precomputed = false;
+    coords_valid = false;
+    uploaded = false;
+  }
+};
+
+namespace nmg {
+
+// Everything a render of rows [r0, r1) of h needs on the GPU (grid, tables),
+// and the device view and kernel that render them (capi.cpp).
+int prepare_view(nm_handle* h, int r0, int r1, DeviceView& v, KernelKind& kind);
+
+}  // namespace nmg

@@ -49,6 +49,34 @@ def setup_gpu(nm, view, path=0, keep64=True):
     return m
 
 
+def zoom_frames(nframes, nr, nc, width0, width1, N0, N1, center=None):
+    """The frames of a zoom video: widths geometric from width0 to width1,
+    N linear from N0 to N1, all into one center (the C2 center by default)."""
+    getcontext().prec = 60
+    cre, cim = center or (C2["cre"], C2["cim"])
+    w0, w1 = Decimal(str(width0)), Decimal(str(width1))
+    out = []
+    for k in range(nframes):
+        t = Decimal(k) / Decimal(max(1, nframes - 1))
+        w = w0 * (w1 / w0) ** t
+        N = int(round(N0 + (N1 - N0) * float(t)))
+        out.append(dict(nr=nr, nc=nc, cre=cre, cim=cim, step=str(w / nc), N=N, tol=1e-10))
+    return out
+
+
+def make_frame(nm, view, sc, deep_path):
+    """A frame handle: the reference's double path where it applies, else
+    `deep_path` with the reference orbit at the view center."""
+    m = nm.Mandelbrot(view["nr"], view["nc"])
+    m.set_view(view["cre"], view["cim"], view["step"], view["step"], view["N"], view["tol"])
+    if sc > 1:
+        m.scaleUp(sc)
+    if not m.useHardware():
+        m.set_path(deep_path)
+        m.set_option(nm.OPT_REFERENCE, nm.REFERENCE_CENTER)
+    return m
+
+
 def sample_positions(nr, nc, n, seed):
     rng = np.random.default_rng(seed)
     k = rng.choice(nr * nc, size=min(n, nr * nc), replace=False)

@@ -65,7 +65,9 @@ enum nm_option {
   NM_OPT_FE32_SINGLE_PASS = 7, /* FE32 in one persistent kernel (default: three passes) */
   NM_OPT_REFERENCE = 8,   /* reference orbit: 0 the reference's probe search
                              (findProbe, mandelbrot.cpp:73-95), 1 the view center */
-  NM_OPT_BATCH_GRAPH = 9  /* batches: 1 replay one captured CUDA graph (default), 0 launch */
+  NM_OPT_BATCH_GRAPH = 9, /* batches: 1 replay one captured CUDA graph (default), 0 launch */
+  NM_OPT_FE32_OVERLAP = 10 /* FE32 passes: 1 render the uncertified samples in FP64 inside
+                              the iteration pass, as they appear (default); 0 after it */
 };
 
 enum nm_stat {
@@ -74,6 +76,7 @@ enum nm_stat {
   NM_STAT_SAMPLES = 2,            /* samples finished in the last render */
   NM_STAT_REBASES = 3,            /* perturbation rebases in the last render */
   NM_STAT_FP64_REWORK = 4,        /* FE32 samples not certified, re-rendered in FP64 */
+  NM_STAT_WAIT_TIMEOUTS = 5,      /* overlapped FP64 rework: bounded waits that ran out (0) */
   NM_STAT_ORBIT_LENGTH = 16,      /* X.size() of the last precompute */
   NM_STAT_PROBE_INDEX = 17,       /* winning probe of findProbe */
   NM_STAT_PRECISION_BITS = 18,    /* arbitrary precision of the view */
@@ -168,7 +171,8 @@ typedef struct nm_batch nm_batch;
 nm_batch* nm_batch_create(int sc);
 void nm_batch_destroy(nm_batch* b);
 int nm_batch_add(nm_batch* b, nm_handle* frame);
-/* NM_OPT_TILE_W, NM_OPT_TILE_H, NM_OPT_CHUNK, NM_OPT_RENORM, NM_OPT_BATCH_GRAPH */
+/* NM_OPT_TILE_W, NM_OPT_TILE_H, NM_OPT_CHUNK, NM_OPT_RENORM, NM_OPT_BATCH_GRAPH,
+   NM_OPT_FE32_OVERLAP */
 int nm_batch_set_option(nm_batch* b, int option, long long value);
 int nm_batch_render(nm_batch* b);
 /* NM_STAT_EXECUTED_ITERS, NM_STAT_SAMPLES, NM_STAT_FP64_REWORK, NM_STAT_KERNEL_NS */

@@ -19,6 +19,7 @@ struct nm_batch {
   std::vector<nm_handle*> frames;
   int tile_w = 16, tile_h = 16, chunk = 32, fe_chunk = 32;
   bool use_graph = true;
+  bool overlap = true;  // FP64 work inside the FE32 iteration pass
 
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -31,7 +32,7 @@ struct nm_batch {
 
   DevBuf<nmg::DeviceView> d_views_fe, d_views_hw, d_views_fp64;
   DevBuf<long long> d_off_fe, d_off_hw, d_off_fp64;
-  DevBuf<char> d_fe_state, d_fe_result;
+  DevBuf<char> d_fe_state;
   DevBuf<unsigned int> d_work, d_rework;
   DevBuf<unsigned long long> d_scratch;
   DevBuf<nmg::ReduceJob> d_reduce;
@@ -65,7 +66,8 @@ enum {
   kHwStats = kHwNext + 1,
   kFp64Next = kHwStats + nmg::STAT_COUNT,
   kFp64Stats = kFp64Next + 1,
-  kBatchWords = kFp64Stats + nmg::STAT_COUNT
+  kFeWarpsDone = kFp64Stats + nmg::STAT_COUNT,
+  kBatchWords = kFeWarpsDone + 1
 };
 
 template <typename T>
@@ -143,7 +145,6 @@ int build(nm_batch* b) {
   if (int rc = upload_vec(b->d_off_fp64, off_fp64, s)) return rc;
   const size_t nfe = (size_t)off_fe.back();
   NM_CUDA(b->d_fe_state.reserve(nfe * nmg::kFeStateBytes));
-  NM_CUDA(b->d_fe_result.reserve(nfe * nmg::kFeResultBytes));
   NM_CUDA(b->d_work.reserve(nfe));
   NM_CUDA(b->d_rework.reserve(nfe));
   NM_CUDA(b->d_scratch.reserve(kBatchWords));
@@ -161,7 +162,6 @@ int build(nm_batch* b) {
   L.fp64 = group(b->d_views_fp64, b->d_off_fp64, off_fp64);
   unsigned long long* w = b->d_scratch.p;
   L.fe_buf.state = reinterpret_cast<nmg::FeState*>(b->d_fe_state.p);
-  L.fe_buf.result = reinterpret_cast<nmg::FeResult*>(b->d_fe_result.p);
   L.fe_buf.work = b->d_work.p;
   L.fe_buf.work_n = w + kWorkN;
   L.fe_ctl = ctl_at(w, kFeNext, kFeStats, 0);
@@ -176,6 +176,11 @@ int build(nm_batch* b) {
   L.fp64_ctl = ctl_at(w, kFp64Next, kFp64Stats, L.fp64.total);
   L.fe_chunk = b->fe_chunk;
   L.chunk = b->chunk;
+  L.overlap = b->overlap;
+  L.overlap_ctl.rework = L.rework_ctl;
+  L.overlap_ctl.fe_warps_done = w + kFeWarpsDone;
+  L.overlap_ctl.timeouts = w + kFeStats + nmg::STAT_WAIT_TIMEOUTS;
+  L.overlap_ctl.chunk = b->chunk;
   L.reduce = b->d_reduce.p;
   L.nreduce = (int)red.size();
   L.reduce_total = red_total;
@@ -257,6 +262,9 @@ int nm_batch_set_option(nm_batch* b, int opt, long long value) {
     case NM_OPT_BATCH_GRAPH:
       b->use_graph = value != 0;
       break;
+    case NM_OPT_FE32_OVERLAP:
+      b->overlap = value != 0;
+      break;
     default:
       return fail(NM_ERR_ARG, "option %d does not apply to a batch", opt);
   }
@@ -333,6 +341,7 @@ int nm_batch_autotune(nm_batch* b, int stride, int* tile_w, int* tile_h, int* re
   nm_batch sub;
   sub.sc = b->sc;
   sub.use_graph = b->use_graph;
+  sub.overlap = b->overlap;
   sub.chunk = b->chunk;
   for (size_t k = 0; k < b->frames.size(); k += (size_t)stride) sub.frames.push_back(b->frames[k]);
   static const int tiles[][2] = {{8, 8}, {16, 16}, {32, 8}, {32, 32}, {64, 16}, {64, 64}};

@@ -248,6 +248,7 @@ nm_handle* nm_copy(const nm_handle* src) {
   h->eps_im_fe = src->eps_im_fe;
   h->reference_mode = src->reference_mode;
   h->fe_single_pass = src->fe_single_pass;
+  h->fe_overlap = src->fe_overlap;
   h->od = src->od;
   h->precomputed = src->precomputed;
   h->coords_valid = src->coords_valid;
@@ -356,6 +357,9 @@ int nm_set_option(nm_handle* h, int opt, long long value) {
     case NM_OPT_FE32_SINGLE_PASS:
       h->fe_single_pass = value != 0;
       return NM_OK;
+    case NM_OPT_FE32_OVERLAP:
+      h->fe_overlap = value != 0;
+      return NM_OK;
     case NM_OPT_REFERENCE:
       if (value != nmg::REFERENCE_PROBES && value != nmg::REFERENCE_CENTER)
         return fail(NM_ERR_ARG, "reference mode %lld", value);
@@ -433,6 +437,21 @@ int nm_upload(nm_handle* h) {
   return do_upload(h);
 }
 
+// The FP64 rework of the FE32 path: the rework list, its length and claim
+// counter, and statistics of its own.
+static nmg::RenderCtl rework_ctl(nm_handle* h, const nmg::RenderCtl& main) {
+  nmg::RenderCtl re = main;
+  re.next = h->d_scratch.p + kNextRework;
+  re.stats = h->d_scratch.p + kStatsRework;
+  re.list = h->d_rework.p;
+  re.count_ptr = h->d_scratch.p + kReworkCount;
+  re.first = 0;
+  re.count = 0;
+  re.rework = nullptr;
+  re.rework_n = nullptr;
+  return re;
+}
+
 int nm_render_rows(nm_handle* h, int r0, int r1, void* stream_arg) {
   if (int rc = check_handle(h)) return rc;
   const int nr = h->view.rows(), nc = h->view.cols();
@@ -468,17 +487,24 @@ int nm_render_rows(nm_handle* h, int r0, int r1, void* stream_arg) {
   NM_CUDA(cudaEventRecord(h->ev[0], s));
   h->timed_iter = false;
   if (kind == nmg::KERNEL_FE32 && !h->fe_single_pass) {
-    // FE32 pass pipeline: FP64 front, FP32 iteration, FP64 smoothing
+    // FE32 pass pipeline: FP64 front, FP32 iteration and smoothing
     NM_CUDA(h->d_fe_state.reserve((size_t)v.total * nmg::kFeStateBytes));
-    NM_CUDA(h->d_fe_result.reserve((size_t)v.total * nmg::kFeResultBytes));
     NM_CUDA(h->d_work.reserve((size_t)v.total));
     nmg::FePassBuffers b;
     b.state = reinterpret_cast<nmg::FeState*>(h->d_fe_state.p);
-    b.result = reinterpret_cast<nmg::FeResult*>(h->d_fe_result.p);
     b.work = h->d_work.p;
     b.work_n = h->d_scratch.p + kWorkCount;
+    nmg::OverlapCtl o;
+    if (h->fe_overlap) {
+      // the FP64 side reads list entries until they differ from the sentinel
+      NM_CUDA(cudaMemsetAsync(h->d_rework.p, 0xff, (size_t)v.total * sizeof(unsigned int), s));
+      o.rework = rework_ctl(h, ctl);
+      o.fe_warps_done = h->d_scratch.p + kFeWarpsDone;
+      o.timeouts = h->d_scratch.p + kStatsMain + nmg::STAT_WAIT_TIMEOUTS;
+      o.chunk = h->chunk;
+    }
     NM_CUDA(nmg::launch_fe32_passes(v, b, ctl, s, h->device, h->blocks, chunk, h->ev[3],
-                                    h->ev[4]));
+                                    h->ev[4], h->fe_overlap ? &o : nullptr));
     h->timed_iter = true;
   } else {
     NM_CUDA(nmg::launch_render(kind, v, ctl, s, blocks, chunk));
@@ -487,15 +513,9 @@ int nm_render_rows(nm_handle* h, int r0, int r1, void* stream_arg) {
   h->timed_rework = kind == nmg::KERNEL_FE32;
   if (kind == nmg::KERNEL_FE32) {
     // Samples the FE32 kernel could not certify: the plain FP64 kernel
-    // renders them again, reading the list and its length from the GPU.
-    nmg::RenderCtl re = ctl;
-    re.next = h->d_scratch.p + kNextRework;
-    re.stats = h->d_scratch.p + kStatsRework;
-    re.list = h->d_rework.p;
-    re.count_ptr = h->d_scratch.p + kReworkCount;
-    re.count = 0;
-    re.rework = nullptr;
-    re.rework_n = nullptr;
+    // renders them again, reading the list and its length from the GPU (after
+    // an overlapped iteration pass: only the entries it left unclaimed).
+    const nmg::RenderCtl re = rework_ctl(h, ctl);
     int rblocks = h->blocks > 0 ? h->blocks : nmg::persistent_blocks(nmg::KERNEL_DELTA64, h->device);
     NM_CUDA(nmg::launch_render(nmg::KERNEL_DELTA64, v, re, s, rblocks, h->chunk));
     NM_CUDA(cudaEventRecord(h->ev[2], s));

@@ -13,6 +13,7 @@ enum StatIndex {
   STAT_SAMPLES = 2,             // samples finished
   STAT_REBASES = 3,             // rebases of the perturbation delta
   STAT_REWORK = 4,              // samples the FE32 kernel handed to the FP64 kernel
+  STAT_WAIT_TIMEOUTS = 5,       // bounded waits of the overlapped rework that ran out
   STAT_COUNT = 8
 };
 
@@ -38,21 +39,35 @@ enum KernelKind { KERNEL_HW = 0, KERNEL_DELTA64 = 1, KERNEL_FE32 = 2 };
 // Buffers of the FE32 pass pipeline (render_fe32.cu), one record per sample
 // index in tile order.
 struct FeState;
-struct FeResult;
 constexpr int kFeStateBytes = 64;
 constexpr int kFeResultBytes = 16;
 struct FePassBuffers {
   FeState* state;              // start state written by the front pass
-  FeResult* result;            // escape iteration and |Y|^2 from the iteration pass
   unsigned int* work;          // samples that need the iteration pass
   unsigned long long* work_n;  // their count (device scratch)
 };
 
-// front pass -> iteration pass (persistent, events around it if given) ->
-// smoothing pass.  ctl carries the counters, the stats and the rework list.
+// The FP64 side of the overlapped iteration pass: warps that render the
+// uncertified samples in FP64 while other warps of the same launch still
+// iterate in FP32 and append to the rework list.  `rework.next` counts the
+// list entries claimed; entries not claimed by the end of the launch are left
+// to a following FP64 launch over the same list and counter.  The list must
+// be filled with kListSentinel before the launch.
+struct OverlapCtl {
+  RenderCtl rework;                  // list, count_ptr, next, stats of the FP64 work
+  unsigned long long* fe_warps_done; // FP32 warps that finished their FP32 work
+  unsigned long long* timeouts;      // waits that ran out (stats word)
+  int chunk;                         // FP64 steps between refills
+};
+constexpr unsigned int kListSentinel = 0xffffffffu;
+
+// front pass -> iteration pass (persistent, events around it if given).  ctl
+// carries the counters, the stats and the rework list; with `overlap` the
+// iteration pass also renders the rework list in FP64 as it grows.
 cudaError_t launch_fe32_passes(const DeviceView& v, const FePassBuffers& b, const RenderCtl& ctl,
                                cudaStream_t stream, int device, int blocks, int chunk,
-                               cudaEvent_t iter_begin, cudaEvent_t iter_end);
+                               cudaEvent_t iter_begin, cudaEvent_t iter_end,
+                               const OverlapCtl* overlap);
 
 // ---- batches of frames (render_batch.cu) ------------------------------------
 // Frames rendered by one kernel: global sample index g of frame f runs over
@@ -76,6 +91,8 @@ struct BatchLaunch {
   BatchGroup fe, hw, fp64;
   FePassBuffers fe_buf;
   RenderCtl fe_ctl, rework_ctl, hw_ctl, fp64_ctl;
+  bool overlap;             // FP64 work inside the FE32 iteration pass
+  OverlapCtl overlap_ctl;   // its rework side (= rework_ctl) and counters
   int fe_chunk, chunk;
   const ReduceJob* reduce;  // [nreduce], device memory
   int nreduce;

@@ -101,6 +101,14 @@ __device__ __forceinline__ bool fe_escape_test(FF yr, FF yi, float yerr, bool& c
   return d > 0.0f;
 }
 
+// The smoothing term of mandelbrot.cpp:133-136, 1 - log2(log|Y|^2 / (2 log 1024)),
+// in FP32 from the float-float |Y|^2 (good to about 2^-22 absolute; the value is
+// stored as a float).  0 for a sample that did not escape.
+__device__ __forceinline__ float fe_smoothing(const DeviceView& v, const FeResult& res) {
+  if (res.it >= v.N) return 0.0f;
+  return 1.0f - log2f(0.5f * logf(res.r2.h + res.r2.l) / (float)v.log_bailout);
+}
+
 __device__ __forceinline__ void fe_renormalise(FeState& st) {
   const float mag = fmaxf(fabsf(st.dr.h), fabsf(st.di.h));
   if (!(mag > 0.0f)) return;
@@ -166,6 +174,11 @@ __device__ __forceinline__ bool fe_scaled_steps(const DeviceView& v, FeState& st
     }
     const float dmag = ldexpf(dl1, st.E);
     if (fabsf(z.hx) + fabsf(z.hy) <= 4.0f * dmag) st.certified = 0;  // |Y| < |delta| possible
+    if (!st.certified) {  // the FP64 kernel renders this sample
+      st.i++;
+      done = true;
+      break;
+    }
     if (st.j == zlast) {  // orbit exhausted: rebase to Z[0], now unscaled
       const float e_abs = ldexpf(st.err, st.E) + kFeUZ * 2048.0f + kFeU * (zl1 + dmag);
       st.dr = yr;
@@ -195,8 +208,10 @@ __device__ __forceinline__ bool fe_scaled_steps(const DeviceView& v, FeState& st
   return false;
 }
 
-// Up to `steps` iterations; true when the sample is finished (res filled,
-// st.certified final).
+// Up to `steps` iterations; true when the sample is finished: either
+// certified with res filled, or uncertified (st.certified == 0), in which case
+// the iteration stops at once and res is not meaningful -- the sample goes to
+// the FP64 kernel.
 __device__ __forceinline__ bool fe_advance(const DeviceView& v, FeState& st, int steps,
                                            FeResult& res, unsigned long long& executed,
                                            unsigned long long& rebases) {
@@ -238,13 +253,23 @@ __device__ __forceinline__ bool fe_advance(const DeviceView& v, FeState& st, int
       // |Y| is below the bailout by more than 2^-11 of it; the hi-part
       // estimate ym is good to 2^-22 (|Z| + |delta|), so the test is decided
       // unless the bound covers the whole gap
-      if (2.0f * (yerr + 0x1p-22f * (zn1 + dn1)) >= kFeBailout - ym) certified = false;
+      if (2.0f * (yerr + 0x1p-22f * (zn1 + dn1)) >= kFeBailout - ym) {
+        certified = false;  // the FP64 kernel renders this sample
+        done = true;
+        i++;
+        break;
+      }
     } else {
       FF r2ff;
       if (fe_escape_test(ff_add(FF{z.hx, z.lx}, dr), ff_add(FF{z.hy, z.ly}, di), yerr,
                          certified, r2ff)) {
         res.it = i;
         res.r2 = r2ff;
+        done = true;
+        i++;
+        break;
+      }
+      if (!certified) {
         done = true;
         i++;
         break;

@@ -60,7 +60,8 @@ constexpr int kNextRework = kStatsMain + nmg::STAT_COUNT;
 constexpr int kStatsRework = kNextRework + 1;
 constexpr int kReworkCount = kStatsRework + nmg::STAT_COUNT;
 constexpr int kWorkCount = kReworkCount + 1;  // FE32 pass pipeline: samples to iterate
-constexpr int kScratchWords = kWorkCount + 1;
+constexpr int kFeWarpsDone = kWorkCount + 1;  // overlapped rework: FP32 warps finished
+constexpr int kScratchWords = kFeWarpsDone + 1;
 }  // namespace scratch
 
 }  // namespace nmg
@@ -112,7 +113,8 @@ struct nm_handle {
   cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   bool timed_rework = false, timed_iter = false;
   bool fe_single_pass = false;  // FE32 in one persistent kernel instead of the passes
-  DevBuf<char> d_fe_state, d_fe_result;
+  bool fe_overlap = true;       // FE32 passes: FP64 rework inside the iteration pass
+  DevBuf<char> d_fe_state;
   DevBuf<unsigned int> d_work;
 
   nm_handle(int nr, int nc) : view(nr, nc) {}

@@ -24,8 +24,10 @@ struct HwJob {
                                                unsigned long long&) {
     int before = st.it;
     bool done = hw_steps(v, st, n, out, sm);
-    executed += (unsigned long long)((done ? out.iterations + (out.iterations < v.N ? 1 : 0)
-                                           : st.it) - before);
+    // an escape returns before st.it is written; after a detected cycle st.it
+    // holds the steps actually run
+    executed += (unsigned long long)((done && out.iterations < v.N ? out.iterations + 1
+                                                                   : st.it) - before);
     return done;
   }
 };

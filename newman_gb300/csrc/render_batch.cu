@@ -3,12 +3,18 @@
 // single CUDA graph.  Frames are grouped by the kernel that renders them:
 //
 //   FE32 frames:  batch_front_kernel (FP64 series front, converged),
-//                 batch_iter_kernel  (FP32 iteration, persistent over all
-//                                     FE32 frames' samples at once),
-//                 batch_finish_kernel (FP64 smoothing),
-//                 batch_list_kernel<Delta64Job> over the uncertified samples;
+//                 batch_overlap_kernel (FP32 iteration and smoothing,
+//                                     persistent over all FE32 frames'
+//                                     samples at once, with the double-path
+//                                     frames and the FP64 rework of the
+//                                     uncertified samples on the FP64 pipe
+//                                     alongside) -- or batch_iter_kernel
+//                                     without the FP64 side,
+//                 batch_list_kernel<Delta64Job> over the uncertified samples
+//                                     (those not yet rendered);
 //   double-path frames (the reference's useHardware views):
-//                 batch_list_kernel<HwJob> over all their samples;
+//                 batch_list_kernel<HwJob> over all their samples (those
+//                                     not yet rendered);
 //   FP64 frames:  batch_list_kernel<Delta64Job> over all their samples;
 //   then batch_reduce_kernel: every frame's multisample mean.
 //
@@ -34,6 +40,16 @@ __device__ __forceinline__ int frame_of(const BatchGroup& g, long long s) {
   }
   return lo;
 }
+
+// The samples of a group of frames for sample_loop / drain_loop.
+struct Frames {
+  const BatchGroup& g;
+  __device__ __forceinline__ const DeviceView& view(int f) const { return g.views[f]; }
+  __device__ __forceinline__ bool locate(long long s, int& f, int& r, int& c) const {
+    f = frame_of(g, s);
+    return sample_rc(g.views[f], s - g.offsets[f], r, c);
+  }
+};
 
 __global__ void __launch_bounds__(256) batch_front_kernel(BatchGroup grp, FePassBuffers b,
                                                           unsigned long long* stats) {
@@ -79,10 +95,8 @@ __global__ void __launch_bounds__(256) batch_front_kernel(BatchGroup grp, FePass
   if (lane == 0 && finished) atomicAdd(&stats[STAT_SAMPLES], finished);
 }
 
-__global__ void __launch_bounds__(kPersistentThreads) batch_iter_kernel(BatchGroup grp,
-                                                                          FePassBuffers b,
-                                                                          RenderCtl ctl,
-                                                                          int chunk) {
+__device__ __forceinline__ void batch_iter_warp(const BatchGroup& grp, const FePassBuffers& b,
+                                                const RenderCtl& ctl, int chunk) {
   const unsigned kFull = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   FeState st;
@@ -119,10 +133,14 @@ __global__ void __launch_bounds__(kPersistentThreads) batch_iter_kernel(BatchGro
     if (!__any_sync(kFull, active)) break;
     if (active) {
       FeResult res;
-      if (fe_advance(grp.views[f], st, chunk, res, executed, rebases)) {
-        res.certified = st.certified;
-        b.result[g] = res;
-        if (!st.certified) {
+      const DeviceView& v = grp.views[f];
+      if (fe_advance(v, st, chunk, res, executed, rebases)) {
+        if (st.certified) {
+          int r = 0, c = 0;
+          sample_rc(v, g - grp.offsets[f], r, c);
+          const float s = fe_smoothing(v, res);
+          store_sample(v, r, c, EscapeValue{res.it, s}, s);
+        } else {  // rendered by the FP64 kernel
           const unsigned long long k = atomicAdd(ctl.rework_n, 1ull);
           ctl.rework[k] = g;
         }
@@ -143,91 +161,42 @@ __global__ void __launch_bounds__(kPersistentThreads) batch_iter_kernel(BatchGro
   }
 }
 
-__global__ void __launch_bounds__(256) batch_finish_kernel(BatchGroup grp, FePassBuffers b) {
-  const unsigned long long n = *b.work_n;
-  for (unsigned long long k = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; k < n;
-       k += (unsigned long long)gridDim.x * blockDim.x) {
-    const unsigned int g = b.work[k];
-    const int f = frame_of(grp, g);
-    const DeviceView& v = grp.views[f];
-    int r = 0, c = 0;
-    sample_rc(v, g - grp.offsets[f], r, c);
-    const FeResult res = b.result[g];
-    const double sm = res.it < v.N ? smoothing_of(ff_to_double(res.r2), v.log_bailout) : 0.0;
-    store_sample(v, r, c, EscapeValue{res.it, (float)sm}, sm);
-  }
+__global__ void __launch_bounds__(kPersistentThreads) batch_iter_kernel(BatchGroup grp,
+                                                                          FePassBuffers b,
+                                                                          RenderCtl ctl,
+                                                                          int chunk) {
+  batch_iter_warp(grp, b, ctl, chunk);
 }
 
-// persistent_loop over the samples of many frames: a range [0, grp.total) or
-// a list of global sample indices (count from device memory).
+// sample_loop over the samples of many frames: a range [0, grp.total) or a
+// list of global sample indices (count from device memory).
 template <class Job>
 __global__ void __launch_bounds__(kPersistentThreads) batch_list_kernel(BatchGroup grp,
                                                                           RenderCtl ctl,
                                                                           int chunk) {
-  const unsigned kFull = 0xffffffffu;
-  const int lane = threadIdx.x & 31;
-  typename Job::State st;
-  bool active = false, exhausted = false;
-  int r = 0, c = 0, f = 0;
-  unsigned long long executed = 0, rebases = 0, finished = 0;
-  const unsigned long long end =
-      ctl.count_ptr ? *ctl.count_ptr : (unsigned long long)ctl.count;
-  for (;;) {
-    for (;;) {
-      const unsigned need = __ballot_sync(kFull, !active && !exhausted);
-      if (!need) break;
-      const int leader = __ffs(need) - 1;
-      unsigned long long base = 0;
-      if (lane == leader) {
-        if (ctl.cancel && *ctl.cancel)
-          base = ~0ull;
-        else
-          base = atomicAdd(ctl.next, (unsigned long long)__popc(need));
-      }
-      base = __shfl_sync(kFull, base, leader);
-      if (!active && !exhausted) {
-        const unsigned long long mine =
-            base == ~0ull ? ~0ull : base + __popc(need & ((1u << lane) - 1));
-        if (mine >= end) {
-          exhausted = true;
-        } else {
-          const long long g = ctl.list ? (long long)ctl.list[mine] : (long long)mine;
-          f = frame_of(grp, g);
-          const DeviceView& v = grp.views[f];
-          if (sample_rc(v, g - grp.offsets[f], r, c)) {
-            EscapeValue out;
-            double sm = 0.0;
-            bool und = false;
-            if (Job::init(v, r, c, st, out, sm, und)) {
-              store_sample(v, r, c, out, sm);
-              finished++;
-            } else {
-              active = true;
-            }
-          }
-        }
-      }
-    }
-    if (!__any_sync(kFull, active)) break;
-    if (active) {
-      EscapeValue out;
-      double sm = 0.0;
-      const DeviceView& v = grp.views[f];
-      if (Job::steps(v, st, chunk, out, sm, executed, rebases)) {
-        store_sample(v, r, c, out, sm);
-        finished++;
-        active = false;
-      }
-    }
+  sample_loop<Job>(Frames{grp}, ctl, chunk);
+}
+
+// The FE32 iteration of every FE32 frame with the FP64 work overlapped (the
+// FP64 pipe is idle under the FP32 iteration): the last warp of every block
+// renders the double-path frames' samples and then the uncertified FE32
+// samples as they are appended; the other warps iterate in FP32 and, when the
+// FP32 work list is exhausted, join the FP64 side.  Capped at 64 registers so
+// that 4 blocks fit on an SM.
+constexpr int kBatchOverlapWarps = 1;
+
+__global__ void __launch_bounds__(kPersistentThreads, 4)
+    batch_overlap_kernel(BatchGroup fe, FePassBuffers b, RenderCtl fe_ctl, BatchGroup hw,
+                         RenderCtl hw_ctl, OverlapCtl o, int chunk) {
+  const int warp = threadIdx.x >> 5;
+  const int fe_warps = kPersistentThreads / 32 - kBatchOverlapWarps;
+  if (warp < fe_warps) {
+    batch_iter_warp(fe, b, fe_ctl, chunk);
+    producer_warp_done(o.fe_warps_done);
   }
-  for (int o = 16; o > 0; o >>= 1) {
-    executed += __shfl_xor_sync(kFull, executed, o);
-    finished += __shfl_xor_sync(kFull, finished, o);
-  }
-  if (lane == 0) {
-    atomicAdd(&ctl.stats[STAT_EXECUTED_ITERS], executed);
-    atomicAdd(&ctl.stats[STAT_SAMPLES], finished);
-  }
+  if (hw.n > 0) sample_loop<HwJob>(Frames{hw}, hw_ctl, o.chunk);
+  drain_loop<Delta64Job>(Frames{fe}, o.rework, o.fe_warps_done,
+                         (unsigned long long)gridDim.x * fe_warps, o.timeouts, o.chunk);
 }
 
 // Multisample mean of every frame (mandelbrot.cpp:320-332), float arithmetic
@@ -273,16 +242,28 @@ int blocks_of(const void* kernel, int threads, int device) {
 cudaError_t launch_batch(const BatchLaunch& L, cudaStream_t s) {
   const int dev = L.device;
   if (L.fe.n > 0 && L.fe.total > 0) {
+    if (L.overlap) {
+      // the FP64 side reads rework entries until they differ from the sentinel
+      cudaError_t e = cudaMemsetAsync(L.fe_ctl.rework, 0xff,
+                                      (size_t)L.fe.total * sizeof(unsigned int), s);
+      if (e != cudaSuccess) return e;
+    }
     batch_front_kernel<<<blocks_of((const void*)batch_front_kernel, 256, dev), 256, 0, s>>>(
         L.fe, L.fe_buf, L.fe_ctl.stats);
-    batch_iter_kernel<<<blocks_of((const void*)batch_iter_kernel, kPersistentThreads, dev),
-                        kPersistentThreads, 0, s>>>(L.fe, L.fe_buf, L.fe_ctl, L.fe_chunk);
-    batch_finish_kernel<<<blocks_of((const void*)batch_finish_kernel, 256, dev), 256, 0, s>>>(
-        L.fe, L.fe_buf);
+    if (L.overlap)
+      batch_overlap_kernel<<<blocks_of((const void*)batch_overlap_kernel, kPersistentThreads,
+                                       dev),
+                             kPersistentThreads, 0, s>>>(L.fe, L.fe_buf, L.fe_ctl, L.hw,
+                                                         L.hw_ctl, L.overlap_ctl, L.fe_chunk);
+    else
+      batch_iter_kernel<<<blocks_of((const void*)batch_iter_kernel, kPersistentThreads, dev),
+                          kPersistentThreads, 0, s>>>(L.fe, L.fe_buf, L.fe_ctl, L.fe_chunk);
     batch_list_kernel<Delta64Job>
         <<<blocks_of((const void*)batch_list_kernel<Delta64Job>, kPersistentThreads, dev),
            kPersistentThreads, 0, s>>>(L.fe, L.rework_ctl, L.chunk);
   }
+  // after an overlapped FE32 pass the double-path range is already used up
+  // (its counter is shared), and this launch only checks that
   if (L.hw.n > 0 && L.hw.total > 0)
     batch_list_kernel<HwJob>
         <<<blocks_of((const void*)batch_list_kernel<HwJob>, kPersistentThreads, dev),

@@ -10,20 +10,20 @@
 //                      appends it to a work list, or finishes it (cardioid,
 //                      escape before the skip point).
 //     fe_iter_kernel   persistent and warp-refilled over the work list, FP32
-//                      only: the delta iteration; appends every sample it could
-//                      not certify to the rework list.
-//     fe_finish_kernel one thread per listed sample, FP64: smoothing from the
-//                      float-float |Y|^2, written to the grid.
+//                      only: the delta iteration and the smoothing term,
+//                      written to the grid; appends every sample it could not
+//                      certify to the rework list.
 //   followed by the plain FP64 kernel over the rework list.  FP64 runs only
 //   in converged warps: GB300 issues FP64 at 1/64 of the FP32 rate, and FP64
 //   inside a refill loop costs a warp's full instruction stream per lane.
 //
 // * The single-pass kernel fe32_kernel: front, iteration and smoothing in one
-//   persistent kernel (FP64 inside the refill loop).  Its scratch is only the
+//   persistent kernel (the FP64 front inside the refill loop).  Its scratch is only the
 //   work counters and the rework list, which lets the allocation-free entry
 //   point (noalloc.cu) run it from a fixed static array.
 #include "engine.hpp"
 #include "fe_core.cuh"
+#include "jobs_fp64.cuh"
 #include "persistent.cuh"
 
 namespace nmg {
@@ -46,8 +46,9 @@ struct FeJob {
                                                unsigned long long& rebases) {
     FeResult res;
     if (!fe_advance(v, st, n, res, executed, rebases)) return false;
-    sm = res.it < v.N ? smoothing_of(ff_to_double(res.r2), v.log_bailout) : 0.0;
-    out = {res.it, (float)sm};
+    const float s = fe_smoothing(v, res);
+    sm = s;
+    out = {res.it, s};
     return true;
   }
   static __device__ __forceinline__ bool certified(const State& st) {
@@ -113,10 +114,9 @@ static_assert(sizeof(FeState) == kFeStateBytes, "FE32 state record");
 static_assert(sizeof(FeResult) == kFeResultBytes, "FE32 result record");
 
 // Persistent and warp-refilled like persistent_loop, over the work list: the
-// start state comes from the front pass, the result goes to the result buffer.
-__global__ void __launch_bounds__(kPersistentThreads) fe_iter_kernel(DeviceView v,
-                                                                       FePassBuffers b,
-                                                                       RenderCtl ctl, int chunk) {
+// start state comes from the front pass, the result goes to the grid.
+__device__ __forceinline__ void fe_iter_warp(const DeviceView& v, const FePassBuffers& b,
+                                             const RenderCtl& ctl, int chunk) {
   const unsigned kFull = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   FeState st;
@@ -152,9 +152,12 @@ __global__ void __launch_bounds__(kPersistentThreads) fe_iter_kernel(DeviceView 
     if (active) {
       FeResult res;
       if (fe_advance(v, st, chunk, res, executed, rebases)) {
-        res.certified = st.certified;
-        b.result[sid] = res;
-        if (!st.certified) {
+        if (st.certified) {
+          int r = 0, c = 0;
+          sample_rc(v, sid, r, c);
+          const float s = fe_smoothing(v, res);
+          store_sample(v, r, c, EscapeValue{res.it, s}, s);
+        } else {  // rendered by the FP64 kernel
           const unsigned long long k = atomicAdd(ctl.rework_n, 1ull);
           ctl.rework[k] = sid;
         }
@@ -175,17 +178,30 @@ __global__ void __launch_bounds__(kPersistentThreads) fe_iter_kernel(DeviceView 
   }
 }
 
-__global__ void __launch_bounds__(256) fe_finish_kernel(DeviceView v, FePassBuffers b) {
-  const unsigned long long n = *b.work_n;
-  for (unsigned long long k = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; k < n;
-       k += (unsigned long long)gridDim.x * blockDim.x) {
-    const unsigned int sid = b.work[k];
-    int r = 0, c = 0;
-    sample_rc(v, sid, r, c);
-    const FeResult res = b.result[sid];
-    const double sm = res.it < v.N ? smoothing_of(ff_to_double(res.r2), v.log_bailout) : 0.0;
-    store_sample(v, r, c, EscapeValue{res.it, (float)sm}, sm);
+__global__ void __launch_bounds__(kPersistentThreads) fe_iter_kernel(DeviceView v,
+                                                                       FePassBuffers b,
+                                                                       RenderCtl ctl, int chunk) {
+  fe_iter_warp(v, b, ctl, chunk);
+}
+
+// The iteration pass with the FP64 rework overlapped: the last warp of every
+// block renders uncertified samples in FP64 (the FP64 pipe is idle under the
+// FP32 iteration) from the start; the other warps iterate in FP32 and, when
+// the FP32 work list is exhausted, join the FP64 side.  Capped at 64
+// registers so that 4 blocks fit on an SM (on the C2 view: 203 ms against
+// 213 ms with two FP64 warps a block and 229 ms uncapped at 3 blocks).
+constexpr int kOverlapWarps = 1;
+
+__global__ void __launch_bounds__(kPersistentThreads, 4) fe_overlap_kernel(
+    DeviceView v, FePassBuffers b, RenderCtl ctl, OverlapCtl o, int chunk) {
+  const int warp = threadIdx.x >> 5;
+  const int fe_warps = kPersistentThreads / 32 - kOverlapWarps;
+  if (warp < fe_warps) {
+    fe_iter_warp(v, b, ctl, chunk);
+    producer_warp_done(o.fe_warps_done);
   }
+  drain_loop<Delta64Job>(OneView{v}, o.rework, o.fe_warps_done,
+                         (unsigned long long)gridDim.x * fe_warps, o.timeouts, o.chunk);
 }
 
 int blocks_for(const void* kernel, int threads, int device) {
@@ -211,7 +227,8 @@ cudaError_t launch_fe32(const DeviceView& v, const RenderCtl& ctl, cudaStream_t 
 
 cudaError_t launch_fe32_passes(const DeviceView& v, const FePassBuffers& b, const RenderCtl& ctl,
                                cudaStream_t stream, int device, int blocks, int chunk,
-                               cudaEvent_t iter_begin, cudaEvent_t iter_end) {
+                               cudaEvent_t iter_begin, cudaEvent_t iter_end,
+                               const OverlapCtl* overlap) {
   const long long total = v.total;
   if (total <= 0) return cudaSuccess;
   fe_front_kernel<<<blocks_for((const void*)fe_front_kernel, 256, device), 256, 0, stream>>>(
@@ -220,12 +237,16 @@ cudaError_t launch_fe32_passes(const DeviceView& v, const FePassBuffers& b, cons
   RenderCtl it = ctl;
   it.list = b.work;
   it.count_ptr = b.work_n;
-  const int iblocks =
-      blocks > 0 ? blocks : blocks_for((const void*)fe_iter_kernel, kPersistentThreads, device);
-  fe_iter_kernel<<<iblocks, kPersistentThreads, 0, stream>>>(v, b, it, chunk);
+  if (overlap) {
+    const int oblocks =
+        blocks > 0 ? blocks : blocks_for((const void*)fe_overlap_kernel, kPersistentThreads, device);
+    fe_overlap_kernel<<<oblocks, kPersistentThreads, 0, stream>>>(v, b, it, *overlap, chunk);
+  } else {
+    const int iblocks =
+        blocks > 0 ? blocks : blocks_for((const void*)fe_iter_kernel, kPersistentThreads, device);
+    fe_iter_kernel<<<iblocks, kPersistentThreads, 0, stream>>>(v, b, it, chunk);
+  }
   if (iter_end) cudaEventRecord(iter_end, stream);
-  fe_finish_kernel<<<blocks_for((const void*)fe_finish_kernel, 256, device), 256, 0, stream>>>(
-      v, b);
   return cudaGetLastError();
 }
 

@@ -75,3 +75,20 @@ def test_batch_autotune_keeps_results(nm, video):
     after = batch.frames_out()
     for a, b in zip(before, after):
         assert np.array_equal(a["iterations"], b["iterations"])
+
+
+def test_batch_overlap_matches_separate_launches(nm, video):
+    """The double-path frames and the FP64 rework inside the FE32 iteration
+    pass give the frames that separate launches give."""
+    views, frames = video
+    out = []
+    for overlap in (1, 0):
+        batch = nm.Batch(sc=2)
+        for f in frames:
+            batch.add(f)
+        batch.set_option(nm.OPT_FE32_OVERLAP, overlap)
+        batch.render()
+        assert batch.stat(nm.STAT_WAIT_TIMEOUTS) == 0
+        out.append(batch.frames_out())
+    for a, b in zip(*out):
+        assert np.array_equal(a, b)

@@ -56,3 +56,22 @@ def test_fe32_counts_every_sample(nm):
     n = b.rows() * b.cols()
     assert b.stat(nm.STAT_SAMPLES) == n
     assert 0 <= b.stat(nm.STAT_FP64_REWORK) <= n
+
+
+def test_overlapped_rework_gives_the_same_grid(nm):
+    """The FP64 rework inside the iteration pass (as uncertified samples
+    appear) gives the grid that the rework after the pass gives."""
+    v = shrink(C2, 96, 160, N=20000)
+    out = []
+    for overlap in (0, 1):
+        m = setup_gpu(nm, v, path=nm.PATH_FE32)
+        m.set_option(nm.OPT_FE32_OVERLAP, overlap)
+        m.precompute()
+        m.render()
+        assert m.stat(nm.STAT_WAIT_TIMEOUTS) == 0
+        assert m.stat(nm.STAT_SAMPLES) == m.rows() * m.cols()
+        out.append((m.grid(), m.smoothing64(), m.stat(nm.STAT_FP64_REWORK)))
+    (g0, s0, n0), (g1, s1, n1) = out
+    assert n0 == n1 and n0 > 0
+    assert np.array_equal(g0, g1)
+    assert np.array_equal(s0, s1)

@@ -89,6 +89,26 @@ def test_interior_view_all_N(nm):
     assert np.all(g["iterations"] == 5000) and np.all(g["smoothing"] == 0)
 
 
+def test_period3_bulb_cycle_detection_bit_exact(nm, oracle_mod):
+    """A view across the period-3 bulb (outside the cardioid test), N 100,000:
+    the double loop's exact cycle detection ends the interior samples early and
+    every escape count still equals the oracle's full-length loop."""
+    v = dict(nr=32, nc=48, sc=1, cre="-0.1225", cim="0.7449", step="0.004", N=100000,
+             tol=1e-10)
+    m = setup_gpu(nm, v)
+    assert m.useHardware()
+    m.render()
+    g = m.grid()
+    o = setup_oracle(oracle_mod, v)
+    it, sm = o.render_rows(0, v["nr"])
+    _compare(g["iterations"], m.smoothing64(), it, sm)
+    interior = (g["iterations"] == v["N"]).mean()
+    assert interior > 0.3
+    # most of the interior samples stopped well before N
+    effective = int(g["iterations"].astype(np.int64).sum())
+    assert m.stat(nm.STAT_EXECUTED_ITERS) < 0.2 * effective
+
+
 def test_multisample_reduce_bit_exact(nm, oracle_mod):
     v = dict(C1, nr=60, nc=80, step="0.0375")
     v["sc"] = 3

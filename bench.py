@@ -433,6 +433,92 @@ def run_video(args):
     print(json.dumps(line), flush=True)
 
 
+def deep_view(k=72):
+    """The view of step k of the seeded boundary-following walk committed in
+    tests/golden/deep_centers.json (start: the C2 center at width 1e-12; each
+    step recenters on the 64x64 render's highest non-maximal escape count and
+    divides the width by 1e4): the center chosen at step k-1 and the width of
+    step k (k = 72: 1e-300)."""
+    with open(os.path.join(ROOT, "tests", "golden", "deep_centers.json")) as f:
+        walk = json.load(f)
+    s = walk["steps"]
+    return s[k - 1]["next_center_re"], s[k - 1]["next_center_im"], s[k]["width"]
+
+
+def run_deep(args):
+    """3840x2160, 1 sample a pixel, width 1e-300, N 1,000,000, reference orbit
+    at 1100 bits at the seeded deep center: the FE32 path over the whole frame
+    (timed), the plain FP64 path over a band of rows for the exactness and the
+    speed comparison (a whole FP64 frame takes minutes)."""
+    import torch
+    from decimal import Decimal, getcontext
+    import newman_gb300 as nm
+    torch.cuda.set_device(0)
+    nr, nc, N, bits = 2160, 3840, 1000000, 1100
+    cre, cim, width = deep_view()
+    getcontext().prec = 340
+    step = str(Decimal(width) / nc)
+
+    def make(path, rows=nr):
+        m = nm.Mandelbrot(rows, nc)
+        m.set_view(cre, cim, step, step, N, TOL, bits)
+        m.set_path(path)
+        m.set_option(nm.OPT_REFERENCE, nm.REFERENCE_CENTER)
+        return m
+
+    m = make(nm.PATH_FE32)
+    t0 = time.perf_counter()
+    m.precompute()
+    precompute_s = time.perf_counter() - t0
+    for _ in range(args.warmup):
+        m.render()
+    times = []
+    with ClockSampler(0) as clocks:
+        for _ in range(args.steps):
+            m.render()
+            times.append(m.stat(nm.STAT_KERNEL_NS) * 1e-6 + m.stat(nm.STAT_REWORK_KERNEL_NS) * 1e-6)
+    ms = float(np.mean(times))
+    g = m.grid()["iterations"]
+    eff = int(g.astype(np.int64).sum())
+    executed = m.stat(nm.STAT_EXECUTED_ITERS)
+    rework = m.stat(nm.STAT_FP64_REWORK)
+    # the plain FP64 path over rows [r0, r1) of the same view and orbit
+    band = max(1, nr // args.deep_band)
+    r0 = (nr - band) // 2
+    fp = m.copy()
+    fp.set_path(nm.PATH_FP64)
+    fp.upload()
+    fp.render_rows(r0, r0 + band)
+    fp.synchronize()
+    fp_ms = fp.stat(nm.STAT_KERNEL_NS) * 1e-6
+    gf = fp.grid()["iterations"][r0:r0 + band]
+    gb = g[r0:r0 + band]
+    exact = float((gf == gb).mean())
+    eff_band = int(gb.astype(np.int64).sum())
+    fe_rate = eff / (ms * 1e-3)
+    fp_rate = eff_band / (fp_ms * 1e-3)
+    line = {
+        "metric": "pixel-iters/s, deep view 3840x2160 at width 1e-300 (FE32 vs plain FP64)",
+        "value": fe_rate, "unit": "pixel-iters/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32 float-float + int exponent",
+        "data": "synthetic view (seeded boundary-following walk, tests/golden/deep_centers.json)",
+        "config": {"workload": "newman C3 deep view", "rows": nr, "cols": nc, "multisample": 1,
+                   "width": width, "max_iter": N, "precision_bits": bits,
+                   "center_re": cre[:40] + "...", "center_im": cim[:40] + "...",
+                   "reference": "orbit at the view center, floatexp series"},
+        "orbit_length": m.stat(nm.STAT_ORBIT_LENGTH), "precompute_s": precompute_s,
+        "executed_iters_per_step": executed, "effective_iters_per_step": eff,
+        "fp64_rework_samples": rework, "max_escape": int(g[g < N].max()) if (g < N).any() else None,
+        "interior_fraction": float((g == N).mean()),
+        "fp64_band": {"rows": [r0, r0 + band], "ms": fp_ms, "value": fp_rate,
+                      "unit": "pixel-iters/s", "exact_iter_fraction_vs_fe32": exact},
+        "speedup_vs_fp64": fe_rate / fp_rate,
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -444,7 +530,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile", type=int, default=0,
                     help="render each path once on a 1/DIV-size crop and exit (ncu case)")
-    ap.add_argument("--workload", default="c2", choices=["c2", "video"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "video", "deep"])
+    ap.add_argument("--deep-band", type=int, default=16,
+                    help="deep workload: the FP64 comparison renders 1/DEEP_BAND of the rows")
     ap.add_argument("--frames", type=int, default=240)
     ap.add_argument("--autotune", action="store_true")
     args = ap.parse_args()
@@ -452,6 +540,8 @@ def main():
         run_reference(args)
     elif args.workload == "video":
         run_video(args)
+    elif args.workload == "deep":
+        run_deep(args)
     else:
         run_ours(args)
 

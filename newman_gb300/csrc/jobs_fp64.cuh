@@ -7,6 +7,7 @@
 #pragma once
 
 #include "pixel_fe64.cuh"
+#include "pixel_xd.cuh"
 
 namespace nmg {
 
@@ -32,9 +33,13 @@ struct HwJob {
   }
 };
 
+// Views with a floatexp series front iterate in FP64 with an unbounded
+// exponent (pixel_xd.cuh); the rest in plain doubles.  The choice is per view,
+// so a warp of one view never diverges on it.
 struct Delta64Job {
-  struct State {
+  union State {
     DeltaState d;
+    DeltaXDState x;
   };
   static constexpr bool kCertifies = false;
   static __device__ __forceinline__ bool certified(const State&) { return true; }
@@ -42,17 +47,21 @@ struct Delta64Job {
                                               EscapeValue& out, double& sm, bool& und) {
     SeriesFront f;
     if (series_front_any(v, r, c, f, out, sm, und)) return true;
-    delta_start(f, st.d);
+    if (v.sa_fe)
+      delta_xd_start(f, st.x);
+    else
+      delta_start(f, st.d);
     return false;
   }
   static __device__ __forceinline__ bool steps(const DeviceView& v, State& st, int n,
                                                EscapeValue& out, double& sm,
                                                unsigned long long& executed,
                                                unsigned long long&) {
-    int before = st.d.i;
-    bool done = delta_steps(v, st.d, n, out, sm);
+    const int before = v.sa_fe ? st.x.i : st.d.i;
+    const bool done = v.sa_fe ? delta_xd_steps(v, st.x, n, out, sm) : delta_steps(v, st.d, n, out, sm);
+    const int after = v.sa_fe ? st.x.i : st.d.i;
     executed += (unsigned long long)((done ? out.iterations + (out.iterations < v.N ? 1 : 0)
-                                           : st.d.i) - before);
+                                           : after) - before);
     return done;
   }
 };

@@ -185,6 +185,15 @@ __global__ void __launch_bounds__(kPersistentThreads) batch_list_kernel(BatchGro
 // that 4 blocks fit on an SM.
 constexpr int kBatchOverlapWarps = 1;
 
+// The FP64 side, out of line: its register pressure (the FP64 series front)
+// then stays out of the FP32 iteration's allocation.
+__device__ __noinline__ void batch_fp64_side(const BatchGroup& fe, const BatchGroup& hw,
+                                             const RenderCtl& hw_ctl, const OverlapCtl& o,
+                                             unsigned long long producers) {
+  if (hw.n > 0) sample_loop<HwJob>(Frames{hw}, hw_ctl, o.chunk);
+  drain_loop<Delta64Job>(Frames{fe}, o.rework, o.fe_warps_done, producers, o.timeouts, o.chunk);
+}
+
 __global__ void __launch_bounds__(kPersistentThreads, 4)
     batch_overlap_kernel(BatchGroup fe, FePassBuffers b, RenderCtl fe_ctl, BatchGroup hw,
                          RenderCtl hw_ctl, OverlapCtl o, int chunk) {
@@ -194,9 +203,7 @@ __global__ void __launch_bounds__(kPersistentThreads, 4)
     batch_iter_warp(fe, b, fe_ctl, chunk);
     producer_warp_done(o.fe_warps_done);
   }
-  if (hw.n > 0) sample_loop<HwJob>(Frames{hw}, hw_ctl, o.chunk);
-  drain_loop<Delta64Job>(Frames{fe}, o.rework, o.fe_warps_done,
-                         (unsigned long long)gridDim.x * fe_warps, o.timeouts, o.chunk);
+  batch_fp64_side(fe, hw, hw_ctl, o, (unsigned long long)gridDim.x * fe_warps);
 }
 
 // Multisample mean of every frame (mandelbrot.cpp:320-332), float arithmetic

@@ -192,6 +192,13 @@ __global__ void __launch_bounds__(kPersistentThreads) fe_iter_kernel(DeviceView 
 // 213 ms with two FP64 warps a block and 229 ms uncapped at 3 blocks).
 constexpr int kOverlapWarps = 1;
 
+// The FP64 side, out of line: its register pressure (the FP64 series front)
+// then stays out of the FP32 iteration's allocation.
+__device__ __noinline__ void overlap_fp64_side(const DeviceView& v, const OverlapCtl& o,
+                                               unsigned long long producers) {
+  drain_loop<Delta64Job>(OneView{v}, o.rework, o.fe_warps_done, producers, o.timeouts, o.chunk);
+}
+
 __global__ void __launch_bounds__(kPersistentThreads, 4) fe_overlap_kernel(
     DeviceView v, FePassBuffers b, RenderCtl ctl, OverlapCtl o, int chunk) {
   const int warp = threadIdx.x >> 5;
@@ -200,8 +207,7 @@ __global__ void __launch_bounds__(kPersistentThreads, 4) fe_overlap_kernel(
     fe_iter_warp(v, b, ctl, chunk);
     producer_warp_done(o.fe_warps_done);
   }
-  drain_loop<Delta64Job>(OneView{v}, o.rework, o.fe_warps_done,
-                         (unsigned long long)gridDim.x * fe_warps, o.timeouts, o.chunk);
+  overlap_fp64_side(v, o, (unsigned long long)gridDim.x * fe_warps);
 }
 
 int blocks_for(const void* kernel, int threads, int device) {

@@ -646,30 +646,69 @@ Pixel get_iterations_fx(View& v, mpf_srcptr y0r, mpf_srcptr y0i, Scratch& s) {
   return {v.N, 0.0};
 }
 
-// MODE_DELTA_FE: the GPU library's FP64 perturbation path on a floatexp view.
+// FP64 with an unbounded exponent: a real m * 2^e with m = 0 or 0.5 <= |m| < 1
+// (frexp's convention).  Each operation rounds its exact result to 53 bits,
+// round-to-nearest-even, as a double operation would without exponent
+// limits: a sum aligns the smaller operand by ldexp (exact for shifts up to
+// 60 bits; beyond that it lies below half an ulp of the larger and the sum
+// is the larger), a product multiplies mantissas in [0.5, 1).  On values in
+// the double range this is the double arithmetic itself.
+struct XR {
+  double m;
+  long e;
+};
+constexpr long kXrZeroExp = -(1L << 40);
+inline XR xr_norm(double x, long e) {
+  if (x == 0.0) return {0.0, kXrZeroExp};
+  int k;
+  double m = std::frexp(x, &k);
+  return {m, e + k};
+}
+inline XR xr_add(XR a, XR b) {
+  if (b.m == 0.0) return a;
+  if (a.m == 0.0) return b;
+  if (a.e < b.e) std::swap(a, b);
+  long d = a.e - b.e;
+  if (d > 60) return a;
+  return xr_norm(a.m + std::ldexp(b.m, (int)-d), a.e);
+}
+inline XR xr_neg(XR a) { return {-a.m, a.e}; }
+inline XR xr_mul(XR a, XR b) { return xr_norm(a.m * b.m, a.e + b.e); }
+inline bool xr_gt(XR a, XR b) {  // a > b for a, b >= 0
+  if (a.m == 0.0) return false;
+  if (b.m == 0.0) return true;
+  return a.e > b.e || (a.e == b.e && a.m > b.m);
+}
+
+// MODE_DELTA_FE: the GPU library's FP64 perturbation path on a floatexp
+// view: delta_steps' operations in FP64 with an unbounded exponent.
 Pixel get_iterations_delta_fx(View& v, mpf_srcptr y0r, mpf_srcptr y0i, Scratch& s,
                               const std::vector<LP>& Z) {
   Pixel out;
   SAStateFX st;
   if (series_front_fx(v, y0r, y0i, s, out, st)) return out;
-  LP dl{fx_re(st.dfound), fx_im(st.dfound)};
-  const LP eps{fx_re(st.eps), fx_im(st.eps)};
+  XR dr = xr_norm(st.dfound.re, st.dfound.e), di = xr_norm(st.dfound.im, st.dfound.e);
+  const XR er = xr_norm(st.eps.re, st.eps.e), ei = xr_norm(st.eps.im, st.eps.e);
+  const XR bail2 = xr_norm(kBailout2, 0);
   size_t j = st.dsize;
   const size_t zlast = Z.size() - 1;
   for (int i = (int)st.dsize; i < v.N; i++) {
-    LP z = Z[j];
-    double tr = 2.0 * z.re + dl.re;
-    double ti = 2.0 * z.im + dl.im;
-    double nre = (tr * dl.re - ti * dl.im) + eps.re;
-    double nim = (tr * dl.im + ti * dl.re) + eps.im;
-    dl = {nre, nim};
+    const LP z = Z[j];
+    XR zr = xr_norm(z.re, 0), zi = xr_norm(z.im, 0);
+    XR tr = xr_add(xr_add(zr, zr), dr);  // 2 z exactly
+    XR ti = xr_add(xr_add(zi, zi), di);
+    XR nre = xr_add(xr_add(xr_mul(tr, dr), xr_neg(xr_mul(ti, di))), er);
+    XR nim = xr_add(xr_add(xr_mul(tr, di), xr_mul(ti, dr)), ei);
+    dr = nre;
+    di = nim;
     j++;
-    LP y{Z[j].re + dl.re, Z[j].im + dl.im};
-    double r2 = y.re * y.re + y.im * y.im;
-    if (r2 > kBailout2) return {i, smoothing_magnitude(r2)};
-    double d2 = dl.re * dl.re + dl.im * dl.im;
-    if (r2 < d2 || j == zlast) {
-      dl = y;
+    XR yr = xr_add(xr_norm(Z[j].re, 0), dr), yi = xr_add(xr_norm(Z[j].im, 0), di);
+    XR r2 = xr_add(xr_mul(yr, yr), xr_mul(yi, yi));
+    if (xr_gt(r2, bail2)) return {i, smoothing_magnitude(std::ldexp(r2.m, (int)r2.e))};
+    XR d2 = xr_add(xr_mul(dr, dr), xr_mul(di, di));
+    if (xr_gt(d2, r2) || j == zlast) {
+      dr = yr;
+      di = yi;
       j = 0;
     }
   }

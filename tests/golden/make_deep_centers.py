@@ -1,18 +1,21 @@
-"""Seeded boundary-following from the C2 center down to width 1e-300 (the
-procedure that defines the deep C3 view), written to deep_centers.json.
+"""Seeded boundary-following from the C2 center down to width 1e-500 (the
+procedure that defines the deep C3 view at 1e-300 and the deep centers of the
+learned-scheduling workload), written to deep_centers.json.
 
-    python tests/golden/make_deep_centers.py [--steps K] [--gpu]
+    python tests/golden/make_deep_centers.py [--steps K] [--to 1e-500] [--gpu]
 
 Start at center -0.743643887037151+0.131825904205330i, width 1e-12.  Repeat:
 render 64x64 samples (N = 1,000,000, series tolerance 1e-10, reference orbit
 at the view center), recenter on the sample with the highest escape count
 below N (ties broken by a seeded RNG), divide the width by 1e4 -- until the
-width is at most 1e-300.  The center is carried as a 320-digit decimal.
+width is at most 1e-500.  The center is carried as a 560-digit decimal
+(every recentering is exact at that precision down to 1e-500).
 
 The renders use the plain FP64 perturbation semantics (series front in
-floatexp below the FP64 range): on the CPU through the oracle's MODE_DELTA_FE,
-or with --gpu through the library's FP64 path, which computes the same escape
-counts bit for bit, so both backends follow the same trajectory.
+floatexp, deltas in FP64 with an unbounded exponent below the FP64 range): on
+the CPU through the oracle's MODE_DELTA_FE, or with --gpu through the
+library's FP64 path, which computes the same escape counts bit for bit, so
+both backends follow the same trajectory.
 """
 import argparse
 import json
@@ -26,7 +29,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
-DIGITS = 320
+DIGITS = 560
 SEED = 2026
 N = 1000000
 GRID = 64
@@ -58,6 +61,7 @@ def render_gpu(cre, cim, step, n):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--to", default="1e-500", help="stop once the width is at most this")
     ap.add_argument("--gpu", action="store_true")
     ap.add_argument("--out", default=os.path.join(HERE, "deep_centers.json"))
     args = ap.parse_args()
@@ -68,7 +72,7 @@ def main():
     render = render_gpu if args.gpu else render_cpu
     steps = []
     for k in range(args.steps):
-        if width < Decimal("1e-300") * Decimal("0.999999"):
+        if width < Decimal(args.to) * Decimal("0.999999"):
             break
         step = width / GRID
         it, bits = render(str(cre), str(cim), str(step), N)
@@ -85,7 +89,7 @@ def main():
         cre, cim = +cre, +cim
         getcontext().prec = DIGITS + 20
         steps.append({"width": str(width), "bits": int(bits), "best": best,
-                      "row": int(r), "col": int(c),
+                      "row": int(r), "col": int(c), "candidates": int(len(cand)),
                       "next_center_re": str(cre), "next_center_im": str(cim)})
         print("width %s bits %d best %d" % (width, bits, best), flush=True)
         width = width / Decimal(10000)

@@ -1,6 +1,6 @@
 """Deep views (series terms outside the FP64 range): the views of the seeded
 boundary-following in tests/golden/deep_centers.json, reference orbit at the
-view center.
+view center, from width 1e-48 down to 1e-360 (below the double range).
 
 * FP64 path against the oracle's MODE_DELTA_FE (same algorithm restated on the
   CPU): escape counts bit-exact, smoothing within 1e-12.
@@ -23,7 +23,7 @@ CENTERS = json.load(open(os.path.join(HERE, "golden", "deep_centers.json")))
 def view_at(k, grid):
     """The view of step k: the center chosen at step k-1, width of step k."""
     from decimal import Decimal, getcontext
-    getcontext().prec = 340
+    getcontext().prec = 600
     s = CENTERS["steps"]
     cre, cim = s[k - 1]["next_center_re"], s[k - 1]["next_center_im"]
     step = str(Decimal(s[k]["width"]) / grid)
@@ -48,7 +48,9 @@ def gpu_render(nm, cre, cim, step, grid, N, path):
     return m
 
 
-@pytest.mark.parametrize("k", [9, 30, 72])
+# k = 80, 87: widths 1e-332 and 1e-360, below the double range (the FP64 path
+# carries its deltas with an unbounded exponent there)
+@pytest.mark.parametrize("k", [9, 30, 72, 80, 87])
 def test_deep_fp64_matches_oracle(nm, oracle_mod, k):
     cre, cim, step = view_at(k, 64)
     N = 300000
@@ -66,7 +68,7 @@ def test_deep_fp64_matches_oracle(nm, oracle_mod, k):
     assert (mp_it == it[:24]).mean() >= 0.75
 
 
-@pytest.mark.parametrize("k", [9, 30, 72])
+@pytest.mark.parametrize("k", [9, 30, 72, 80, 87])
 def test_deep_fe32_matches_fp64(nm, k):
     cre, cim, step = view_at(k, 256)
     N = 300000

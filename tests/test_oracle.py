@@ -128,3 +128,21 @@ def test_delta_mode_equals_reference_on_hw_free_front(oracle_mod):
     it_d, sm_d = o.render_rows(0, nr, oracle_mod.MODE_DELTA)
     it_r, sm_r = o.render_rows(0, nr, oracle_mod.MODE_REF)
     assert (it_d == it_r).mean() >= 0.95
+
+
+def test_unbounded_exponent_delta_equals_plain_fp64_in_range(oracle_mod):
+    """MODE_DELTA_FE (floatexp series front, FP64 deltas with an unbounded
+    exponent) gives MODE_DELTA's results bit for bit on a view inside the
+    double range: the floatexp front equals the FP64 front there, and the
+    unbounded-exponent arithmetic equals double arithmetic on values that
+    never leave the double range."""
+    g = np.load(os.path.join(HERE, "golden", "deep_view.npz"))
+    nr, nc = int(g["nr"]), int(g["nc"])
+    o = oracle_mod.OracleView(nr, nc)
+    o.set_view(str(g["center_re"]), str(g["center_im"]), str(g["step"]), str(g["step"]),
+               int(g["N"]))
+    o.precompute()
+    it_d, sm_d = o.render_rows(0, nr, oracle_mod.MODE_DELTA)
+    it_x, sm_x = o.render_rows(0, nr, oracle_mod.MODE_DELTA_FE)
+    assert np.array_equal(it_d, it_x)
+    assert np.array_equal(sm_d, sm_x)

@@ -519,6 +519,166 @@ def run_deep(args):
     print(json.dumps(line), flush=True)
 
 
+def learned_views(count=10, seed=5):
+    """The deep views of the learned-scheduling workload: stopping widths
+    log-uniform in [1e-500, 1e-50] (seeded); each view has its stopping width
+    and is centered where the seeded boundary-following walk
+    (tests/golden/deep_centers.json) stands when its width first reaches the
+    stopping width."""
+    with open(os.path.join(ROOT, "tests", "golden", "deep_centers.json")) as f:
+        steps = json.load(f)["steps"]
+    from decimal import Decimal
+    rng = np.random.default_rng(seed)
+    out = []
+    for e in sorted(rng.uniform(50.0, 500.0, count)):
+        log_w = [Decimal(s["width"]).log10() for s in steps]
+        k = next((i for i in range(1, len(steps)) if log_w[i] <= Decimal(-e)), len(steps) - 1)
+        ce = int(np.ceil(e))
+        width = "%.12fe-%d" % (10.0 ** (ce - e), ce)
+        out.append({"stop": "1e-%.2f" % e, "k": k, "width": width,
+                    "cre": steps[k - 1]["next_center_re"], "cim": steps[k - 1]["next_center_im"]})
+    return out
+
+
+def tile_log(nm, m, sc, tile_px=32, preview_px=8):
+    """Per-tile features (from a preview with one sample per preview_px x
+    preview_px pixels) and the logged per-tile work of one whole render of m,
+    on tiles of tile_px x tile_px pixels."""
+    tile = tile_px * sc
+    m.set_option(nm.OPT_TILE_W, tile)
+    m.set_option(nm.OPT_TILE_H, tile)
+    m.set_option(nm.OPT_LOG_TILE_COSTS, 1)
+    m.render()
+    costs = m.tile_costs().astype(np.float64).ravel()
+    m.set_option(nm.OPT_LOG_TILE_COSTS, 0)
+    f = preview_px * sc
+    p = m.preview(f)
+    if not p.useHardware() and p.stat(nm.STAT_ORBIT_LENGTH) == 0:
+        p.precompute()
+    p.render()
+    return p.tile_features(tile // f, tile // f), costs
+
+
+def centred_log(costs):
+    y = np.log2(1.0 + costs)
+    return (y - y.mean()).astype(np.float32)
+
+
+def spearman(a, b):
+    ra = np.argsort(np.argsort(a)).astype(np.float64)
+    rb = np.argsort(np.argsort(b)).astype(np.float64)
+    return float(np.corrcoef(ra, rb)[0, 1]) if ra.std() > 0 and rb.std() > 0 else None
+
+
+def run_learned(args):
+    """Learned-scheduled deep renders: the cost model trained on the tile costs
+    of the C1, C2 and C3 views, then 10 seeded deep views (3840x2160, 2x2
+    samples, N 2,000,000) rendered with the static tile order and with the
+    predicted longest-first order (preview and prediction included in its
+    time); the images must be identical."""
+    import torch
+    from decimal import Decimal, getcontext
+    import newman_gb300 as nm
+    torch.cuda.set_device(0)
+    getcontext().prec = 700
+    t_all = time.perf_counter()
+
+    # training data: tile costs logged on the C1, C2 and C3 views
+    def view(nr, nc, sc, cre, cim, width, N, bits=0, path=nm.PATH_FE32):
+        m = nm.Mandelbrot(nr, nc)
+        step = str(Decimal(width) / nc)
+        m.set_view(cre, cim, step, step, N, TOL, bits)
+        if sc > 1:
+            m.scaleUp(sc)
+        if not m.useHardware():
+            m.set_path(path)
+            m.set_option(nm.OPT_REFERENCE, nm.REFERENCE_CENTER)
+            m.precompute()
+        return m
+
+    dcre, dcim, dwidth = deep_view()
+    train_views = [("C1", view(480, 640, 1, "-0.75", "0", "3.0", 1024), 1),
+                   ("C2", view(NR, NC, SC, CENTER[0], CENTER[1], WIDTH, N_ITER), SC),
+                   ("C3", view(2160, 3840, 1, dcre, dcim, dwidth, 1000000, 1100), 1)]
+    X, Y, train_info = [], [], {}
+    for name, m, sc in train_views:
+        feats, costs = tile_log(nm, m, sc)
+        X.append(feats)
+        Y.append(centred_log(costs))
+        train_info[name] = {"tiles": int(len(costs)), "cost_spread_log2": float(np.ptp(Y[-1]))}
+        del m
+    X, Y = np.concatenate(X), np.concatenate(Y)
+    model = nm.CostModel(seed=2026)
+    t0 = time.perf_counter()
+    loss = model.train(X, Y, epochs=args.epochs, lr=2e-3)
+    train_s = time.perf_counter() - t0
+    var = float(np.var(Y))
+
+    # the deep views
+    nr, nc, sc, N = 2160, 3840, 2, 2000000
+    rows, t_static, t_learned, t_oracle, t_over = [], 0.0, 0.0, 0.0, 0.0
+    identical = True
+    for vw in learned_views():
+        m = view(nr, nc, sc, vw["cre"], vw["cim"], vw["width"], N)
+        feats, costs = tile_log(nm, m, sc)  # tile size set, costs for the error report
+
+        def timed_render(order):
+            m.set_tile_order(order)
+            m.render()  # warm
+            ts = []
+            for _ in range(args.steps):
+                m.render()
+                ts.append(m.stat(nm.STAT_KERNEL_NS) * 1e-6 + m.stat(nm.STAT_REWORK_KERNEL_NS) * 1e-6)
+            return float(np.mean(ts)), m.grid()
+
+        ms_static, g_static = timed_render(None)
+        # learned order: preview, features, prediction, sort -- all timed
+        t0 = time.perf_counter()
+        p = m.preview(8 * sc)
+        p.render()
+        f = p.tile_features(32 // 8, 32 // 8)
+        pred = model.predict(f)
+        order = np.argsort(-pred, kind="stable").astype(np.int32)
+        over_ms = (time.perf_counter() - t0) * 1e3
+        ms_learned, g_learned = timed_render(order)
+        ms_oracle, g_oracle = timed_render(np.argsort(-costs, kind="stable").astype(np.int32))
+        same = bool(np.array_equal(g_static, g_learned) and np.array_equal(g_static, g_oracle))
+        identical &= same
+        y = centred_log(costs)
+        err = pred - pred.mean() - y
+        rows.append({"width": vw["width"], "stop": vw["stop"], "orbit_length": m.stat(nm.STAT_ORBIT_LENGTH),
+                     "ms_static": ms_static, "ms_learned": ms_learned, "ms_overhead": over_ms,
+                     "ms_cost_order": ms_oracle, "identical": same,
+                     "spearman": spearman(pred, costs), "mae_log2": float(np.abs(err).mean()),
+                     "cost_spread_log2": float(np.ptp(y))})
+        t_static += ms_static
+        t_learned += ms_learned
+        t_over += over_ms
+        t_oracle += ms_oracle
+        del m, p
+    speedup = t_static / (t_learned + t_over)
+    sp = [r["spearman"] for r in rows if r["spearman"] is not None]
+    line = {
+        "metric": "learned tile order: render speedup over the static order, 10 deep views",
+        "value": speedup, "unit": "x", "n_gpus": 1, "steps": args.steps, "warmup": 1,
+        "ms_per_step": t_learned + t_over, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32 float-float + int exponent; model fp16 weights, fp32 accumulate",
+        "data": "synthetic views (seeded boundary-following walk, tests/golden/deep_centers.json)",
+        "config": {"workload": "newman C5 learned-scheduled deep renders", "rows": nr, "cols": nc,
+                   "multisample": sc, "max_iter": N, "views": len(rows), "tile_px": 32,
+                   "preview_px": 8, "model": "18-64-64-64-1 ReLU MLP",
+                   "train_views": train_info, "epochs": args.epochs},
+        "train": {"tiles": int(len(Y)), "loss": loss, "target_variance": var, "seconds": train_s},
+        "ms_static_total": t_static, "ms_learned_total": t_learned, "ms_overhead_total": t_over,
+        "ms_cost_order_total": t_oracle, "speedup_without_overhead": t_static / t_learned,
+        "speedup_cost_order": t_static / t_oracle, "bit_identical": identical,
+        "prediction": {"spearman_mean": float(np.mean(sp)) if sp else None,
+                       "mae_log2_mean": float(np.mean([r["mae_log2"] for r in rows]))},
+        "views": rows, "wall_s": time.perf_counter() - t_all,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -530,7 +690,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile", type=int, default=0,
                     help="render each path once on a 1/DIV-size crop and exit (ncu case)")
-    ap.add_argument("--workload", default="c2", choices=["c2", "video", "deep"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "video", "deep", "learned"])
+    ap.add_argument("--epochs", type=int, default=400, help="learned workload: training epochs")
     ap.add_argument("--deep-band", type=int, default=16,
                     help="deep workload: the FP64 comparison renders 1/DEEP_BAND of the rows")
     ap.add_argument("--frames", type=int, default=240)
@@ -542,6 +703,8 @@ def main():
         run_video(args)
     elif args.workload == "deep":
         run_deep(args)
+    elif args.workload == "learned":
+        run_learned(args)
     else:
         run_ours(args)
 

@@ -66,8 +66,9 @@ enum nm_option {
   NM_OPT_REFERENCE = 8,   /* reference orbit: 0 the reference's probe search
                              (findProbe, mandelbrot.cpp:73-95), 1 the view center */
   NM_OPT_BATCH_GRAPH = 9, /* batches: 1 replay one captured CUDA graph (default), 0 launch */
-  NM_OPT_FE32_OVERLAP = 10 /* FE32 passes: 1 render the uncertified samples in FP64 inside
+  NM_OPT_FE32_OVERLAP = 10, /* FE32 passes: 1 render the uncertified samples in FP64 inside
                               the iteration pass, as they appear (default); 0 after it */
+  NM_OPT_LOG_TILE_COSTS = 11 /* 1: whole-grid renders log every tile's work (nm_get_tile_costs) */
 };
 
 enum nm_stat {
@@ -92,6 +93,11 @@ enum nm_stat {
 nm_handle* nm_create(int nr, int nc);
 /* Value copy (the reference copies Mandelbrot objects, viewer.cpp:193,251). */
 nm_handle* nm_copy(const nm_handle* src);
+/* No reference counterpart: the same view on a grid `factor` times coarser in
+   each direction (rows and columns must be multiples of it).  A precomputed
+   view with its reference orbit at the view center shares that orbit and its
+   series: the preview is ready to render without nm_precompute. */
+nm_handle* nm_preview(const nm_handle* src, int factor);
 void nm_destroy(nm_handle* h);
 const char* nm_last_error(void);
 
@@ -156,6 +162,42 @@ int nm_zoom(nm_handle* h, float scale);                            /* mandelbrot
 int nm_zoom_at(nm_handle* h, float scale, int r, int c, int sc);   /* mandelbrot.cpp:304-316 */
 int nm_load_legacy(nm_handle* h, const char* path);                /* mandelbrot.cpp:19-35 */
 int nm_save(const nm_handle* h, const char* path);                 /* viewer.cpp:12-23 */
+
+/* ---- learned tile scheduling (no reference counterpart) ---------------------
+   Tiles are the render's tiles of NM_OPT_TILE_W x NM_OPT_TILE_H samples,
+   row-major ids over the whole grid.  nm_set_tile_order sets the order in
+   which whole-grid renders hand them out (a permutation; NULL restores
+   row-major); the image does not depend on it.  With NM_OPT_LOG_TILE_COSTS a
+   whole-grid render logs each tile's work: the iteration steps its samples
+   ran, FP64 steps counted 8 (FP32-step equivalents). */
+int nm_tiles(nm_handle* h, int* tiles_x, int* tiles_y);
+int nm_set_tile_order(nm_handle* h, const int* order, int n);
+int nm_get_tile_costs(nm_handle* h, unsigned long long* out, int n);
+
+/* Features of the tiles of a rendered preview (nm_preview), tile_w x tile_h
+   preview samples each, NM_COST_FEATURES floats per tile, row-major tiles:
+   a 16-bin histogram of x = (log2(1 + it) - lo) / (hi - lo) over the tile's
+   samples (lo, hi: the preview's escaping samples' range; x = 1 at N), then
+   the mean and the max of x. */
+#define NM_COST_FEATURES 18
+#define NM_COST_PARAMS 9601
+int nm_tile_features(nm_handle* preview, int tile_w, int tile_h, float* out, int ntiles);
+
+/* Cost model: MLP 18 -> 64 -> 64 -> 64 -> 1 (ReLU), FP16 weights with FP32
+   accumulation in hand-written kernels; FP32 master parameters (NM_COST_PARAMS,
+   layout W1[64][18] b1 W2[64][64] b2 W3[64][64] b3 W4[64] b4) trained with
+   Adam on the mean squared error.  Inputs / outputs are host arrays. */
+typedef struct nm_costmodel nm_costmodel;
+nm_costmodel* nm_cost_model_create(unsigned long long seed);
+void nm_cost_model_destroy(nm_costmodel* m);
+int nm_cost_model_params(nm_costmodel* m, float* out, int n);
+int nm_cost_model_set_params(nm_costmodel* m, const float* in, int n);
+int nm_cost_model_predict(nm_costmodel* m, const float* features, int n, float* out);
+/* Gradient of mean((y - target)^2) over the n rows, FP32, parameter layout. */
+int nm_cost_model_gradient(nm_costmodel* m, const float* features, const float* targets, int n,
+                           float* grad, float* loss);
+int nm_cost_model_train(nm_costmodel* m, const float* features, const float* targets, int n,
+                        int epochs, float lr, float* loss);
 
 /* Batches: many frames rendered together, e.g. every frame of a zoom video,
    each frame a handle with its own view, orbit, series skip and N (no

@@ -20,12 +20,15 @@ NM_OK, NM_ERR_ARG, NM_ERR_PARSE, NM_ERR_STATE, NM_ERR_CUDA, NM_ERR_CANCELLED, NM
     NM_ERR_UNSUPPORTED = range(8)
 PATH_REFERENCE, PATH_FP64, PATH_FE32 = 0, 1, 2
 OPT_TILE_W, OPT_TILE_H, OPT_CHUNK, OPT_KEEP_SMOOTH64, OPT_THREADS, OPT_BLOCKS, OPT_RENORM, \
-    OPT_FE32_SINGLE_PASS, OPT_REFERENCE, OPT_BATCH_GRAPH, OPT_FE32_OVERLAP = range(11)
+    OPT_FE32_SINGLE_PASS, OPT_REFERENCE, OPT_BATCH_GRAPH, OPT_FE32_OVERLAP, \
+    OPT_LOG_TILE_COSTS = range(12)
 REFERENCE_PROBES, REFERENCE_CENTER = 0, 1
 STAT_CARDIOID_UNDECIDED, STAT_EXECUTED_ITERS, STAT_SAMPLES, STAT_REBASES, STAT_FP64_REWORK, \
     STAT_WAIT_TIMEOUTS = range(6)
 STAT_ORBIT_LENGTH, STAT_PROBE_INDEX, STAT_PRECISION_BITS, STAT_PRECOMPUTE_US = 16, 17, 18, 19
 STAT_KERNEL_NS, STAT_REWORK_KERNEL_NS, STAT_ITER_KERNEL_NS = 20, 21, 22
+
+COST_FEATURES, COST_PARAMS = 18, 9601
 
 ESCAPE_DTYPE = np.dtype([("iterations", "<i4"), ("smoothing", "<f4")])
 
@@ -40,6 +43,10 @@ EXPORTS = (
     "nm_zoom_at", "nm_load_legacy", "nm_save", "nm_peak_flops", "nm_render_fe32_noalloc",
     "nm_batch_create", "nm_batch_destroy", "nm_batch_add", "nm_batch_set_option",
     "nm_batch_render", "nm_batch_get_stat", "nm_batch_frames", "nm_batch_autotune",
+    "nm_preview", "nm_tiles", "nm_set_tile_order", "nm_get_tile_costs", "nm_tile_features",
+    "nm_cost_model_create", "nm_cost_model_destroy", "nm_cost_model_params",
+    "nm_cost_model_set_params", "nm_cost_model_predict", "nm_cost_model_gradient",
+    "nm_cost_model_train",
 )
 
 
@@ -115,6 +122,18 @@ def load_library(path=LIB_PATH):
         "nm_batch_get_stat": (i32, [vp, i32, P(ll)]),
         "nm_batch_frames": (i32, [vp, vp]),
         "nm_batch_autotune": (i32, [vp, i32, P(i32), P(i32), P(i32)]),
+        "nm_preview": (vp, [vp, i32]),
+        "nm_tiles": (i32, [vp, P(i32), P(i32)]),
+        "nm_set_tile_order": (i32, [vp, vp, i32]),
+        "nm_get_tile_costs": (i32, [vp, vp, i32]),
+        "nm_tile_features": (i32, [vp, i32, i32, vp, i32]),
+        "nm_cost_model_create": (vp, [ctypes.c_ulonglong]),
+        "nm_cost_model_destroy": (None, [vp]),
+        "nm_cost_model_params": (i32, [vp, vp, i32]),
+        "nm_cost_model_set_params": (i32, [vp, vp, i32]),
+        "nm_cost_model_predict": (i32, [vp, vp, i32, vp]),
+        "nm_cost_model_gradient": (i32, [vp, vp, vp, i32, vp, vp]),
+        "nm_cost_model_train": (i32, [vp, vp, vp, i32, i32, ctypes.c_float, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -183,6 +202,54 @@ class Batch:
         return w.value, h.value, rn.value
 
 
+class CostModel:
+    """The tile cost model (nm_cost_model_*): MLP 18 -> 64 -> 64 -> 64 -> 1 with
+    FP16 weights and FP32 accumulation, trained with Adam on the GPU."""
+
+    def __init__(self, seed=0):
+        L = load_library()
+        self._m = L.nm_cost_model_create(int(seed))
+        if not self._m:
+            raise NewmanError(NM_ERR_CUDA, L.nm_last_error().decode())
+
+    def __del__(self):
+        m, self._m = getattr(self, "_m", None), None
+        if m and _lib is not None:
+            _lib.nm_cost_model_destroy(m)
+
+    def params(self):
+        out = np.empty(COST_PARAMS, np.float32)
+        _check(_lib.nm_cost_model_params(self._m, out.ctypes.data, out.size))
+        return out
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        _check(_lib.nm_cost_model_set_params(self._m, p.ctypes.data, p.size))
+
+    def predict(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, COST_FEATURES)
+        out = np.empty(len(x), np.float32)
+        _check(_lib.nm_cost_model_predict(self._m, x.ctypes.data, len(x), out.ctypes.data))
+        return out
+
+    def gradient(self, x, t):
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, COST_FEATURES)
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        g = np.empty(COST_PARAMS, np.float32)
+        loss = ctypes.c_float()
+        _check(_lib.nm_cost_model_gradient(self._m, x.ctypes.data, t.ctypes.data, len(x),
+                                           g.ctypes.data, ctypes.byref(loss)))
+        return g, loss.value
+
+    def train(self, x, t, epochs, lr=1e-3):
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, COST_FEATURES)
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        loss = ctypes.c_float()
+        _check(_lib.nm_cost_model_train(self._m, x.ctypes.data, t.ctypes.data, len(x),
+                                        int(epochs), float(lr), ctypes.byref(loss)))
+        return loss.value
+
+
 def peak_flops(kind):
     """Measured FP32 FMA (0), FP64 FMA (1) or FP64 unfused (2) flop/s."""
     v = ctypes.c_double(0.0)
@@ -210,6 +277,48 @@ class Mandelbrot:
         if not h:
             raise NewmanError(NM_ERR_CUDA, _lib.nm_last_error().decode())
         return Mandelbrot(_handle=h)
+
+    # ---- learned tile scheduling (no reference counterpart) -----------------
+    def preview(self, factor):
+        """The same view on a grid `factor` times coarser (nm_preview); shares a
+        precomputed view-center orbit."""
+        h = _lib.nm_preview(self._h, int(factor))
+        if not h:
+            raise NewmanError(NM_ERR_ARG, _lib.nm_last_error().decode())
+        return Mandelbrot(_handle=h)
+
+    def tiles(self):
+        """(tiles_x, tiles_y) of the whole grid at the current tile size."""
+        tx, ty = ctypes.c_int(), ctypes.c_int()
+        _check(_lib.nm_tiles(self._h, ctypes.byref(tx), ctypes.byref(ty)))
+        return tx.value, ty.value
+
+    def set_tile_order(self, order=None):
+        """Hand-out order of the tiles (a permutation of row-major tile ids);
+        None restores row-major."""
+        if order is None:
+            _check(_lib.nm_set_tile_order(self._h, None, 0))
+            return
+        o = np.ascontiguousarray(order, dtype=np.int32)
+        _check(_lib.nm_set_tile_order(self._h, o.ctypes.data, o.size))
+
+    def tile_costs(self):
+        """Per-tile work of the last whole-grid render (NM_OPT_LOG_TILE_COSTS),
+        shaped (tiles_y, tiles_x)."""
+        tx, ty = self.tiles()
+        out = np.empty(tx * ty, np.uint64)
+        _check(_lib.nm_get_tile_costs(self._h, out.ctypes.data, out.size))
+        return out.reshape(ty, tx)
+
+    def tile_features(self, tile_w, tile_h):
+        """Features of this (rendered preview) grid's tiles of tile_w x tile_h
+        samples: (tiles, COST_FEATURES) float32, row-major tiles."""
+        tx = (self.cols() + tile_w - 1) // tile_w
+        ty = (self.rows() + tile_h - 1) // tile_h
+        out = np.empty((tx * ty, COST_FEATURES), np.float32)
+        _check(_lib.nm_tile_features(self._h, int(tile_w), int(tile_h), out.ctypes.data,
+                                     tx * ty))
+        return out
 
     # ---- fields -----------------------------------------------------------
     @property

@@ -207,6 +207,17 @@ int nmg::prepare_view(nm_handle* h, int r0, int r1, nmg::DeviceView& v, nmg::Ker
   }
   v.grid = h->grid.p;
   v.smooth64 = h->keep_smooth64 ? h->smooth64.p : nullptr;
+  const bool whole = r0 == 0 && r1 == nr;
+  if (whole && !h->tile_order.empty() && h->tile_order_w == h->tile_w &&
+      h->tile_order_h == h->tile_h &&
+      (long long)h->tile_order.size() == (long long)v.tiles_x * v.tiles_y) {
+    if (!h->tile_order_uploaded) {
+      if (int rc = upload(h->d_tile_order, h->tile_order, h->stream)) return rc;
+      NM_CUDA(cudaStreamSynchronize(h->stream));
+      h->tile_order_uploaded = true;
+    }
+    v.tile_order = h->d_tile_order.p;
+  }
   kind = hw ? nmg::KERNEL_HW : (h->path == NM_PATH_FE32 ? nmg::KERNEL_FE32 : nmg::KERNEL_DELTA64);
   return NM_OK;
 }
@@ -249,6 +260,10 @@ nm_handle* nm_copy(const nm_handle* src) {
   h->reference_mode = src->reference_mode;
   h->fe_single_pass = src->fe_single_pass;
   h->fe_overlap = src->fe_overlap;
+  h->tile_order = src->tile_order;
+  h->tile_order_w = src->tile_order_w;
+  h->tile_order_h = src->tile_order_h;
+  h->log_costs = src->log_costs;
   h->od = src->od;
   h->precomputed = src->precomputed;
   h->coords_valid = src->coords_valid;
@@ -359,6 +374,9 @@ int nm_set_option(nm_handle* h, int opt, long long value) {
       return NM_OK;
     case NM_OPT_FE32_OVERLAP:
       h->fe_overlap = value != 0;
+      return NM_OK;
+    case NM_OPT_LOG_TILE_COSTS:
+      h->log_costs = value != 0;
       return NM_OK;
     case NM_OPT_REFERENCE:
       if (value != nmg::REFERENCE_PROBES && value != nmg::REFERENCE_CENTER)
@@ -472,6 +490,13 @@ int nm_render_rows(nm_handle* h, int r0, int r1, void* stream_arg) {
     ctl.rework = h->d_rework.p;
     ctl.rework_n = h->d_scratch.p + kReworkCount;
   }
+  if (h->log_costs && r0 == 0 && r1 == nr) {
+    const long long tiles = (long long)v.tiles_x * v.tiles_y;
+    NM_CUDA(h->d_tile_cost.reserve((size_t)tiles));
+    NM_CUDA(cudaMemsetAsync(h->d_tile_cost.p, 0, (size_t)tiles * 8, s));
+    v.tile_cost = h->d_tile_cost.p;
+    h->cost_tiles = tiles;
+  }
   *h->cancel_host = 0;
   h->expected_samples = (long long)(r1 - r0) * nc;
   NM_CUDA(cudaMemsetAsync(h->d_scratch.p, 0, kScratchWords * 8, s));
@@ -546,6 +571,80 @@ int nm_render(nm_handle* h) {
 int nm_compute_row(nm_handle* h, int r) {
   if (int rc = nm_render_rows(h, r, r + 1, nullptr)) return rc;
   return nm_synchronize(h);
+}
+
+int nm_tiles(nm_handle* h, int* tiles_x, int* tiles_y) {
+  if (int rc = check_handle(h)) return rc;
+  if (!tiles_x || !tiles_y) return fail(NM_ERR_ARG, "null output");
+  *tiles_x = (h->view.cols() + h->tile_w - 1) / h->tile_w;
+  *tiles_y = (h->view.rows() + h->tile_h - 1) / h->tile_h;
+  return NM_OK;
+}
+
+int nm_set_tile_order(nm_handle* h, const int* order, int n) {
+  if (int rc = check_handle(h)) return rc;
+  if (!order || n == 0) {
+    h->tile_order.clear();
+    return NM_OK;
+  }
+  int tx = 0, ty = 0;
+  nm_tiles(h, &tx, &ty);
+  if ((long long)n != (long long)tx * ty)
+    return fail(NM_ERR_ARG, "tile order of %d entries for %d x %d tiles", n, tx, ty);
+  std::vector<char> seen((size_t)n, 0);
+  for (int k = 0; k < n; k++) {
+    if (order[k] < 0 || order[k] >= n || seen[(size_t)order[k]])
+      return fail(NM_ERR_ARG, "tile order is not a permutation (entry %d = %d)", k, order[k]);
+    seen[(size_t)order[k]] = 1;
+  }
+  h->tile_order.assign(order, order + n);
+  h->tile_order_w = h->tile_w;
+  h->tile_order_h = h->tile_h;
+  h->tile_order_uploaded = false;
+  return NM_OK;
+}
+
+int nm_get_tile_costs(nm_handle* h, unsigned long long* out, int n) {
+  if (int rc = check_handle(h)) return rc;
+  if (!out) return fail(NM_ERR_ARG, "null output");
+  if (h->cost_tiles == 0 || !h->stream)
+    return fail(NM_ERR_STATE, "no logged render (set NM_OPT_LOG_TILE_COSTS, render the whole grid)");
+  if ((long long)n != h->cost_tiles)
+    return fail(NM_ERR_ARG, "%d entries for a log of %lld tiles", n, h->cost_tiles);
+  NM_CUDA(cudaStreamSynchronize(h->stream));
+  NM_CUDA(cudaMemcpy(out, h->d_tile_cost.p, (size_t)n * 8, cudaMemcpyDeviceToHost));
+  return NM_OK;
+}
+
+nm_handle* nm_preview(const nm_handle* src, int factor) {
+  if (!src || factor < 1) {
+    fail(NM_ERR_ARG, "preview of %s at factor %d", src ? "a view" : "a null handle", factor);
+    return nullptr;
+  }
+  if (src->view.rows() % factor || src->view.cols() % factor) {
+    fail(NM_ERR_ARG, "grid %d x %d is not a multiple of the preview factor %d", src->view.rows(),
+         src->view.cols(), factor);
+    return nullptr;
+  }
+  std::unique_ptr<nm_handle> h(new nm_handle(1, 1));
+  h->view = src->view;
+  h->view.scale_down(factor);
+  h->path = src->path;
+  h->chunk = src->chunk;
+  h->threads = src->threads;
+  h->renorm = src->renorm;
+  h->reference_mode = src->reference_mode;
+  h->fe_overlap = src->fe_overlap;
+  if (src->precomputed && src->reference_mode == nmg::REFERENCE_CENTER) {
+    // the orbit at the view center and its series do not depend on the grid:
+    // only the per-row / per-column tables are the preview's own
+    h->od = src->od;
+    if (ensure_coords(h.get()) != NM_OK) return nullptr;
+    h->view.eps_tables(h->od, h->eps_re, h->eps_im);
+    if (!h->od.sa_fp64_ok) h->view.eps_tables_fe(h->eps_re_fe, h->eps_im_fe);
+    h->precomputed = true;
+  }
+  return h.release();
 }
 
 int nm_cancel(nm_handle* h) {

@@ -117,6 +117,17 @@ struct nm_handle {
   DevBuf<char> d_fe_state;
   DevBuf<unsigned int> d_work;
 
+  // scheduling: the order in which whole-grid renders hand out their tiles (a
+  // permutation of the tiles at tile_order_w x tile_order_h; empty: row-major)
+  // and the per-tile cost log of the last whole-grid render
+  std::vector<int32_t> tile_order;
+  int tile_order_w = 0, tile_order_h = 0;
+  bool tile_order_uploaded = false;
+  DevBuf<int32_t> d_tile_order;
+  bool log_costs = false;
+  DevBuf<unsigned long long> d_tile_cost;
+  long long cost_tiles = 0;
+
   nm_handle(int nr, int nc) : view(nr, nc) {}
   ~nm_handle() {
     for (cudaEvent_t e : ev)

@@ -14,6 +14,7 @@ namespace nmg {
 struct HwJob {
   using State = HwState;
   static constexpr bool kCertifies = false;
+  static constexpr int kCostWeight = kCostFp64Step;
   static __device__ __forceinline__ bool certified(const State&) { return true; }
   static __device__ __forceinline__ bool init(const DeviceView& v, int r, int c, State& st,
                                               EscapeValue& out, double& sm, bool& und) {
@@ -42,6 +43,7 @@ struct Delta64Job {
     DeltaXDState x;
   };
   static constexpr bool kCertifies = false;
+  static constexpr int kCostWeight = kCostFp64Step;
   static __device__ __forceinline__ bool certified(const State&) { return true; }
   static __device__ __forceinline__ bool init(const DeviceView& v, int r, int c, State& st,
                                               EscapeValue& out, double& sm, bool& und) {

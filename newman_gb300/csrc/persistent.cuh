@@ -40,6 +40,12 @@ struct OneView {
   }
 };
 
+// Adds a finished sample's work to its tile's entry of the cost log.
+__device__ __forceinline__ void log_cost(const DeviceView& v, int r, int c,
+                                         unsigned long long steps, int weight) {
+  if (v.tile_cost && steps) atomicAdd(&v.tile_cost[tile_at(v, r, c)], steps * weight);
+}
+
 template <class Job, class Src>
 __device__ __forceinline__ void sample_loop(const Src& src, const RenderCtl& ctl, int chunk) {
   const unsigned kFull = 0xffffffffu;
@@ -48,7 +54,7 @@ __device__ __forceinline__ void sample_loop(const Src& src, const RenderCtl& ctl
   bool active = false, exhausted = false;
   int r = 0, c = 0, f = 0;
   long long sid = 0;
-  unsigned long long executed = 0, rebases = 0, finished = 0, undecided = 0;
+  unsigned long long executed = 0, rebases = 0, finished = 0, undecided = 0, exec0 = 0;
   const unsigned long long end =
       ctl.count_ptr ? *ctl.count_ptr : (unsigned long long)ctl.count;
 
@@ -83,6 +89,7 @@ __device__ __forceinline__ void sample_loop(const Src& src, const RenderCtl& ctl
               finished++;
             } else {
               active = true;
+              exec0 = executed;
             }
             undecided += und ? 1 : 0;
           }
@@ -100,6 +107,7 @@ __device__ __forceinline__ void sample_loop(const Src& src, const RenderCtl& ctl
         } else {
           store_sample(src.view(f), r, c, out, sm);
         }
+        log_cost(src.view(f), r, c, executed - exec0, Job::kCostWeight);
         finished++;
         active = false;
       }
@@ -194,7 +202,7 @@ __device__ __forceinline__ void drain_loop(const Src& src, const RenderCtl& ctl,
   bool active = false, closed = false;
   int r = 0, c = 0, f = 0;
   unsigned idle = 0;
-  unsigned long long executed = 0, rebases = 0, finished = 0, undecided = 0, lost = 0;
+  unsigned long long executed = 0, rebases = 0, finished = 0, undecided = 0, lost = 0, exec0 = 0;
   for (;;) {
     const unsigned need = __ballot_sync(kFull, !active);
     if (need && !closed) {
@@ -233,6 +241,7 @@ __device__ __forceinline__ void drain_loop(const Src& src, const RenderCtl& ctl,
               finished++;
             } else {
               active = true;
+              exec0 = executed;
             }
             undecided += und ? 1 : 0;
           }
@@ -250,6 +259,7 @@ __device__ __forceinline__ void drain_loop(const Src& src, const RenderCtl& ctl,
       double sm = 0.0;
       if (Job::steps(src.view(f), st, chunk, out, sm, executed, rebases)) {
         store_sample(src.view(f), r, c, out, sm);
+        log_cost(src.view(f), r, c, executed - exec0, Job::kCostWeight);
         finished++;
         active = false;
       }

@@ -103,7 +103,7 @@ __device__ __forceinline__ void batch_iter_warp(const BatchGroup& grp, const FeP
   unsigned int g = 0;
   int f = 0;
   bool active = false, exhausted = false;
-  unsigned long long executed = 0, rebases = 0, finished = 0;
+  unsigned long long executed = 0, rebases = 0, finished = 0, exec0 = 0;
   const unsigned long long end = *ctl.count_ptr;
   for (;;) {
     const unsigned need = __ballot_sync(kFull, !active && !exhausted);
@@ -127,6 +127,7 @@ __device__ __forceinline__ void batch_iter_warp(const BatchGroup& grp, const FeP
           st = b.state[g];
           f = st.pad_[0];
           active = true;
+          exec0 = executed;
         }
       }
     }
@@ -135,9 +136,10 @@ __device__ __forceinline__ void batch_iter_warp(const BatchGroup& grp, const FeP
       FeResult res;
       const DeviceView& v = grp.views[f];
       if (fe_advance(v, st, chunk, res, executed, rebases)) {
+        int r = 0, c = 0;
+        sample_rc(v, g - grp.offsets[f], r, c);
+        log_cost(v, r, c, executed - exec0, 1);
         if (st.certified) {
-          int r = 0, c = 0;
-          sample_rc(v, g - grp.offsets[f], r, c);
           const float s = fe_smoothing(v, res);
           store_sample(v, r, c, EscapeValue{res.it, s}, s);
         } else {  // rendered by the FP64 kernel

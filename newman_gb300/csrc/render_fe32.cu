@@ -33,6 +33,7 @@ namespace {
 struct FeJob {
   using State = FeState;
   static constexpr bool kCertifies = true;
+  static constexpr int kCostWeight = 1;
   static __device__ __forceinline__ bool init(const DeviceView& v, int r, int c, State& st,
                                               EscapeValue& out, double& sm, bool& und) {
     SeriesFront f;
@@ -122,7 +123,7 @@ __device__ __forceinline__ void fe_iter_warp(const DeviceView& v, const FePassBu
   FeState st;
   unsigned int sid = 0;
   bool active = false, exhausted = false;
-  unsigned long long executed = 0, rebases = 0, finished = 0;
+  unsigned long long executed = 0, rebases = 0, finished = 0, exec0 = 0;
   const unsigned long long end = *ctl.count_ptr;
   for (;;) {
     const unsigned need = __ballot_sync(kFull, !active && !exhausted);
@@ -145,6 +146,7 @@ __device__ __forceinline__ void fe_iter_warp(const DeviceView& v, const FePassBu
           sid = ctl.list[mine];
           st = b.state[sid];
           active = true;
+          exec0 = executed;
         }
       }
     }
@@ -152,15 +154,16 @@ __device__ __forceinline__ void fe_iter_warp(const DeviceView& v, const FePassBu
     if (active) {
       FeResult res;
       if (fe_advance(v, st, chunk, res, executed, rebases)) {
+        int r = 0, c = 0;
+        sample_rc(v, sid, r, c);
         if (st.certified) {
-          int r = 0, c = 0;
-          sample_rc(v, sid, r, c);
           const float s = fe_smoothing(v, res);
           store_sample(v, r, c, EscapeValue{res.it, s}, s);
         } else {  // rendered by the FP64 kernel
           const unsigned long long k = atomicAdd(ctl.rework_n, 1ull);
           ctl.rework[k] = sid;
         }
+        log_cost(v, r, c, executed - exec0, 1);
         finished++;
         active = false;
       }

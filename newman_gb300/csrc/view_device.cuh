@@ -82,18 +82,35 @@ struct DeviceView {
 
   EscapeValue* grid;       // [nr*nc]
   double* smooth64;        // optional [nr*nc] unrounded smoothing
+
+  // Scheduling (whole-grid launches only; both may be null).
+  const int32_t* tile_order;     // [tiles_x*tiles_y] hand-out position -> tile (row-major id)
+  unsigned long long* tile_cost; // [tiles_x*tiles_y] work of each tile's samples, in
+                                 // FP32-step equivalents (kCostFp64Step per FP64 step)
 };
 
+// An FP64 step counted in FP32-step equivalents for the tile cost log: GB300
+// issues FP64 at about 1/64 of the FP32 rate, and an FP64 step has 7-14 FP64
+// operations against about 140 FP32 instructions for an FE32 step.
+constexpr int kCostFp64Step = 8;
+
 // Sample index in tile order -> (r, c); false for padding past the grid edge.
+// With a tile order, the k-th tile handed out is tile_order[k].
 NM_HD bool sample_rc(const DeviceView& v, int64_t s, int& r, int& c) {
   const int64_t per_tile = (int64_t)v.tile_w * v.tile_h;
   const int64_t tile = s / per_tile;
   const int t = (int)(s - tile * per_tile);
-  const int ty = (int)(tile / v.tiles_x);
-  const int tx = (int)(tile - (int64_t)ty * v.tiles_x);
+  const int64_t id = v.tile_order ? (int64_t)v.tile_order[tile] : tile;
+  const int ty = (int)(id / v.tiles_x);
+  const int tx = (int)(id - (int64_t)ty * v.tiles_x);
   r = v.row0 + ty * v.tile_h + t / v.tile_w;
   c = tx * v.tile_w + t % v.tile_w;
   return r < v.row1 && c < v.nc;
+}
+
+// Row-major id of the tile holding sample (r, c).
+NM_HD int64_t tile_at(const DeviceView& v, int r, int c) {
+  return (int64_t)((r - v.row0) / v.tile_h) * v.tiles_x + c / v.tile_w;
 }
 
 }  // namespace nmg

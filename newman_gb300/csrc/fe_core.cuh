@@ -12,7 +12,18 @@
 // absolute error of delta against exact arithmetic from the same start,
 //     e' = 2|Y| e + e^2 + u (|t||delta| + |eps|) + u_z 2|Z||delta|,
 // u the float-float rounding, u_z the float-float representation of the FP64
-// orbit.  The FP64 path's own rounding is 2^-9 of that bound, so when every
+// orbit.  u: one component of the float-float multiply-add (ff32.cuh) rounds
+// 8 times into its low word; with unit roundoff 2^-24 and every low-word term
+// at most 2^-24 of the products P = |a.h b.h| + |a'.h b'.h|, the worst case
+// (terms aligned, partial sums at their largest) is 30 * 2^-48 P +
+// 8 * 2^-48 |eps|, plus 2^-48 P for the dropped lo*lo products; the two
+// components' P add up to |t.h|_1 |delta.h|_1, so u = 1.125 * 2^-43.  u_z:
+// Z in float-float is within (2^-48 + 2^-52) |Z| of the exact orbit (the
+// FP64 orbit is mpf_get_d's truncation), and t = 2Z + delta rounds by at
+// most 2^-46 (2|Z| + |delta|); the bound carries u_z (2|Z| + |delta|)|delta|
+// with u_z = 2^-45.  Every operation on the bound rounds upward, so over
+// millions of steps it never falls below the exact recurrence.
+// The FP64 path's own rounding is below 2^-6 of that bound, so when every
 // bailout test of a sample is decided by more than twice the bound, both paths
 // take the same branch at every test and return the same escape count.  A
 // sample with a test inside the band ends "uncertified".  The escape test
@@ -27,10 +38,15 @@
 namespace nmg {
 
 constexpr int kFeScaledBelow = -60;   // delta kept as mantissa * 2^E below 2^-60
-constexpr float kFeU = 0x1p-44f;      // float-float rounding per step (generous)
-constexpr float kFeUZ = 0x1p-47f;     // float-float representation of Z
+constexpr float kFeU = 0x1.2p-43f;    // float-float multiply-add rounding per step (worst case)
+constexpr float kFeUZ = 0x1p-45f;     // Z's representation and the rounding of t = 2Z + delta
 constexpr float kFeBailout = 1024.0f;       // mandelbrot.cpp:58
 constexpr float kFeBailout2 = 1048576.0f;   // mandelbrot.cpp:59
+
+// Arithmetic on error bounds, rounded upward.
+__device__ __forceinline__ float up_add(float a, float b) { return __fadd_ru(a, b); }
+__device__ __forceinline__ float up_mul(float a, float b) { return __fmul_ru(a, b); }
+__device__ __forceinline__ float up_fma(float a, float b, float c) { return __fmaf_ru(a, b, c); }
 
 struct alignas(16) FeState {
   FF dr, di;      // delta * 2^-E
@@ -72,10 +88,19 @@ __device__ __forceinline__ void fe_start(const SeriesFront& f, FeState& st) {
   st.di = ff_from_double(scalbn(f.dfound.im, f.d_e - E));
   st.er = ff_from_double(scalbn(f.eps.re, f.eps_e - E));
   st.ei = ff_from_double(scalbn(f.eps.im, f.eps_e - E));
-  st.err = kFeU * (fabsf(st.dr.h) + fabsf(st.di.h));
+  st.err = up_mul(kFeU, up_add(fabsf(st.dr.h), fabsf(st.di.h)));
   st.j = f.dsize;
   st.i = f.dsize;
   st.certified = 1;
+}
+
+// sqrt(x) from the hardware reciprocal square root (relative error below
+// 2^-21; 0 for x = 0).
+__device__ __forceinline__ float approx_sqrt(float x) {
+  return x > 0.0f ? x * rsqrtf(x) : 0.0f;
+}
+__device__ __forceinline__ float approx_norm(float x, float y) {
+  return approx_sqrt(fmaf(x, x, y * y));
 }
 
 // x^2 + y^2 in float-float.
@@ -97,7 +122,8 @@ __device__ __forceinline__ bool fe_escape_test(FF yr, FF yi, float yerr, bool& c
   r2 = ff_norm2(yr, yi);
   const float d = (r2.h - kFeBailout2) + r2.l;  // r2.h - 2^20 is exact near 2^20
   // | |Y| - 1024 | <= 2 yerr  <=>  | |Y|^2 - 2^20 | <= (2048 + 2 yerr) 2 yerr
-  if (fabsf(d) <= (2048.0f + 2.0f * yerr) * 2.0f * yerr + 0x1p-40f * r2.h) certified = false;
+  if (fabsf(d) <= up_fma(up_fma(2.0f, yerr, 2048.0f), up_mul(2.0f, yerr), up_mul(0x1p-40f, r2.h)))
+    certified = false;
   return d > 0.0f;
 }
 
@@ -145,12 +171,20 @@ __device__ __forceinline__ bool fe_scaled_steps(const DeviceView& v, FeState& st
     const FF sd_i = st.E < -140 ? FF{0.f, 0.f} : ff_scale(st.di, st.E);
     const FF tr = ff_add(FF{2.0f * z.hx, 2.0f * z.lx}, sd_r);
     const FF ti = ff_add(FF{2.0f * z.hy, 2.0f * z.ly}, sd_i);
-    const float zl1 = fabsf(z.hx) + fabsf(z.hy), dl1 = fabsf(st.dr.h) + fabsf(st.di.h);
+    const float zl1 = up_add(fabsf(z.hx), fabsf(z.hy)), dl1 = up_add(fabsf(st.dr.h), fabsf(st.di.h));
     FF nr, ni;
     ff_cmul_add(tr, ti, st.dr, st.di, st.er, st.ei, nr, ni);
-    st.err = fmaf(2.0f * zl1, st.err,
-                  kFeU * fmaf(fabsf(tr.h) + fabsf(ti.h), dl1, fabsf(st.er.h) + fabsf(st.ei.h)) +
-                      kFeUZ * 2.0f * zl1 * dl1);
+    {
+      // scaled units: e' = 2 (|Z| + |delta|) e + e^2 2^E + u (|t||delta| + |eps|)
+      //                     + u_z (2|Z| + |delta|) |delta|
+      const float dmag = fmaxf(ldexpf(dl1, st.E), 0x1p-126f);
+      const float amp = up_add(up_mul(2.0f, up_add(zl1, dmag)),
+                               fmaxf(ldexpf(st.err, st.E), 0x1p-126f));
+      const float loc = up_fma(kFeU, up_fma(up_add(fabsf(tr.h), fabsf(ti.h)), dl1,
+                                            up_add(fabsf(st.er.h), fabsf(st.ei.h))),
+                               up_mul(kFeUZ, up_mul(up_fma(2.0f, zl1, dmag), dl1)));
+      st.err = up_fma(amp, st.err, loc);
+    }
     st.dr = nr;
     st.di = ni;
     st.j++;
@@ -159,7 +193,8 @@ __device__ __forceinline__ bool fe_scaled_steps(const DeviceView& v, FeState& st
     const FF yr = ff_add(FF{z.hx, z.lx}, st.E < -140 ? FF{0.f, 0.f} : ff_scale(st.dr, st.E));
     const FF yi = ff_add(FF{z.hy, z.ly}, st.E < -140 ? FF{0.f, 0.f} : ff_scale(st.di, st.E));
     if (zm2 > kFeBailout2 * (1.0f - 0x1p-10f)) {
-      const float yerr = ldexpf(st.err, st.E) + kFeUZ * (fabsf(z.hx) + fabsf(z.hy));
+      const float yerr = up_add(fmaxf(ldexpf(st.err, st.E), 0x1p-126f),
+                                up_mul(kFeUZ, up_add(fabsf(z.hx), fabsf(z.hy))));
       bool cert = st.certified != 0;
       FF r2;
       if (fe_escape_test(yr, yi, yerr, cert, r2)) {
@@ -180,7 +215,8 @@ __device__ __forceinline__ bool fe_scaled_steps(const DeviceView& v, FeState& st
       break;
     }
     if (st.j == zlast) {  // orbit exhausted: rebase to Z[0], now unscaled
-      const float e_abs = ldexpf(st.err, st.E) + kFeUZ * 2048.0f + kFeU * (zl1 + dmag);
+      const float e_abs = up_add(up_add(fmaxf(ldexpf(st.err, st.E), 0x1p-126f), kFeUZ * 2048.0f),
+                                 up_mul(kFeU, up_add(zl1, dmag)));
       st.dr = yr;
       st.di = yi;
       st.er = ff_scale(st.er, st.E);
@@ -220,23 +256,27 @@ __device__ __forceinline__ bool fe_advance(const DeviceView& v, FeState& st, int
   const int stop = min(v.N, st.i + steps);
   const int start = st.i;
   const float lo_band = kFeBailout2 * (1.0f - 0x1p-10f);
-  const float eps_l1 = fabsf(st.er.h) + fabsf(st.ei.h);
+  const float eps_l1 = up_add(fabsf(st.er.h), fabsf(st.ei.h));
   const FF er = st.er, ei = st.ei;
   FF dr = st.dr, di = st.di;
   float err = st.err;
   int j = st.j, i = st.i;
   bool certified = st.certified != 0;
   ZFF z = fe_load_z(v, j);
-  // |Y| of the current state (for the error bound's amplification 2|Y|)
-  float ym = sqrtf(fmaf(z.hx + dr.h, z.hx + dr.h, (z.hy + di.h) * (z.hy + di.h)));
+  // |Y| of the current state (for the error bound's amplification 2|Y|),
+  // from the hardware reciprocal square root: within 2^-21 of |Y_h|, which
+  // the 2^-20 (|Z| + |delta|) margins below cover together with the hi parts'
+  // own error (2^-22)
+  float ym = approx_norm(z.hx + dr.h, z.hy + di.h);
   bool done = false;
   for (; i < stop; i++) {
     const FF tr = ff_add(FF{2.0f * z.hx, 2.0f * z.lx}, dr);
     const FF ti = ff_add(FF{2.0f * z.hy, 2.0f * z.ly}, di);
-    const float zl1 = fabsf(z.hx) + fabsf(z.hy), dl1 = fabsf(dr.h) + fabsf(di.h);
-    const float ym_up = ym + 0x1p-22f * (zl1 + dl1);
-    err = fmaf(2.0f * ym_up + err, err,
-               kFeU * fmaf(fabsf(tr.h) + fabsf(ti.h), dl1, eps_l1) + kFeUZ * 2.0f * zl1 * dl1);
+    const float zl1 = up_add(fabsf(z.hx), fabsf(z.hy)), dl1 = up_add(fabsf(dr.h), fabsf(di.h));
+    const float ym_up = up_fma(0x1p-20f, up_add(zl1, dl1), ym);
+    const float loc = up_fma(kFeU, up_fma(up_add(fabsf(tr.h), fabsf(ti.h)), dl1, eps_l1),
+                             up_mul(kFeUZ, up_mul(up_fma(2.0f, zl1, dl1), dl1)));
+    err = up_fma(up_fma(2.0f, ym_up, err), err, loc);  // 2|Y| e + e^2 + local rounding
     FF nr, ni;
     ff_cmul_add(tr, ti, dr, di, er, ei, nr, ni);
     dr = nr;
@@ -245,15 +285,15 @@ __device__ __forceinline__ bool fe_advance(const DeviceView& v, FeState& st, int
     z = fe_load_z(v, j);
     const float yr = z.hx + dr.h, yi = z.hy + di.h;
     const float r2 = fmaf(yr, yr, yi * yi);
-    ym = sqrtf(r2);
-    const float zn1 = fabsf(z.hx) + fabsf(z.hy), dn1 = fabsf(dr.h) + fabsf(di.h);
+    ym = approx_sqrt(r2);
+    const float zn1 = up_add(fabsf(z.hx), fabsf(z.hy)), dn1 = up_add(fabsf(dr.h), fabsf(di.h));
     // error of Y = Z + delta held in float-float (the rebase value)
-    const float yerr = err + kFeUZ * zn1 + kFeU * (zn1 + dn1);
+    const float yerr = up_add(err, up_fma(kFeUZ, zn1, up_mul(kFeU, up_add(zn1, dn1))));
     if (r2 <= lo_band) {
-      // |Y| is below the bailout by more than 2^-11 of it; the hi-part
-      // estimate ym is good to 2^-22 (|Z| + |delta|), so the test is decided
-      // unless the bound covers the whole gap
-      if (2.0f * (yerr + 0x1p-22f * (zn1 + dn1)) >= kFeBailout - ym) {
+      // |Y| is below the bailout by more than 2^-11 of it; the estimate ym
+      // is good to 2^-20 (|Z| + |delta|), so the test is decided unless the
+      // bound covers the whole gap
+      if (up_mul(2.0f, up_fma(0x1p-20f, up_add(zn1, dn1), yerr)) >= __fsub_rd(kFeBailout, ym)) {
         certified = false;  // the FP64 kernel renders this sample
         done = true;
         i++;
@@ -284,7 +324,7 @@ __device__ __forceinline__ bool fe_advance(const DeviceView& v, FeState& st, int
       err = yerr;
       j = 0;
       z = fe_load_z(v, 0);
-      ym = sqrtf(fmaf(dr.h, dr.h, di.h * di.h));
+      ym = approx_norm(dr.h, di.h);
       rebases++;
     }
   }

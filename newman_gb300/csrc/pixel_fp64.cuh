@@ -165,6 +165,38 @@ NM_HD bool same_bits(double a, double b) {
 #endif
 }
 
+// 2 x exactly (the reference's mul(2.0, x)): an exponent increment for a
+// normal x whose double stays finite, else the multiply.
+NM_HD double twice_(double x) {
+#if defined(__CUDA_ARCH__)
+  const int hi = __double2hiint(x);
+  const int e = (hi >> 20) & 0x7ff;
+  if (e >= 1 && e <= 0x7fd) return __hiloint2double(hi + 0x00100000, __double2loint(x));
+#endif
+  return mul_(2.0, x);
+}
+
+// Biased exponent field of x (0 for zero and subnormals).
+NM_HD int exp_field(double x) {
+#if defined(__CUDA_ARCH__)
+  return (__double2hiint(x) >> 20) & 0x7ff;
+#else
+  long long b;
+  std::memcpy(&b, &x, 8);
+  return (int)((b >> 52) & 0x7ff);
+#endif
+}
+
+// True when |(yr, yi)| exceeds |(dr, di)| by so much that the FP64 values of
+// yr^2 + yi^2 and dr^2 + di^2 compare greater, whatever their rounding: the
+// larger component of Y is at least 4 times the larger of delta's (|Y|^2 >=
+// 16 max^2 > 2 |delta|^2, far beyond 2^-52).
+NM_HD bool clearly_larger(double yr, double yi, double dr, double di) {
+  const int ay = exp_field(yr), by = exp_field(yi), ad = exp_field(dr), bd = exp_field(di);
+  const int ey = ay > by ? ay : by, ed = ad > bd ? ad : bd;
+  return ey >= ed + 2 && ey > 0;
+}
+
 // r2 > bailout2 for r2 >= 0 and bailout2 > 0, on the bit patterns.
 NM_HD bool above_bits(double r2, double bailout2) {
 #if defined(__CUDA_ARCH__)
@@ -368,6 +400,9 @@ NM_HD bool series_front(const DeviceView& v, int r, int c, SeriesFront& f, Escap
 //     t = 2 Z[j] + delta;  delta = t * delta + eps;  j += 1;  Y = Z[j] + delta
 // and the pixel rebases to Z[0] (delta = Y, j = 0) when |Y| < |delta| or the
 // orbit is exhausted.  `i` counts like getIterations' continuation (:212).
+// The doubling is an exponent increment, the comparisons work on bit
+// patterns, and |delta|^2 is formed only when |Y| is not clearly larger: 13
+// FP64 operations a step instead of 20, with the same results.
 struct DeltaState {
   double dr, di, er, ei;
   int32_t j, i;
@@ -398,8 +433,8 @@ NM_HD bool delta_steps(const DeviceView& v, DeltaState& st, int steps, EscapeVal
   const int stop = (v.N - i < steps) ? v.N : i + steps;
   for (; i < stop; i++) {
     const Dbl2 z = v.z[j];
-    double tr = add_(mul_(2.0, z.x), dr);
-    double ti = add_(mul_(2.0, z.y), di);
+    double tr = add_(twice_(z.x), dr);
+    double ti = add_(twice_(z.y), di);
     double nre = add_(sub_(mul_(tr, dr), mul_(ti, di)), st.er);
     double nim = add_(add_(mul_(tr, di), mul_(ti, dr)), st.ei);
     dr = nre;
@@ -408,13 +443,16 @@ NM_HD bool delta_steps(const DeviceView& v, DeltaState& st, int steps, EscapeVal
     const Dbl2 zn = v.z[j];
     double yr = add_(zn.x, dr), yi = add_(zn.y, di);
     double r2 = add_(mul_(yr, yr), mul_(yi, yi));
-    if (r2 > v.bailout2) {
+    if (above_bits(r2, v.bailout2)) {
       sm = smoothing_of(r2, v.log_bailout);
       out = {i, (float)sm};
       return true;
     }
-    double d2 = add_(mul_(dr, dr), mul_(di, di));
-    if (r2 < d2 || j == zlast) {
+    // the rebase test r2 < d2, evaluated only when |Y| is not clearly larger
+    bool rebase = j == zlast;
+    if (!rebase && !clearly_larger(yr, yi, dr, di))
+      rebase = above_bits(add_(mul_(dr, dr), mul_(di, di)), r2);
+    if (rebase) {
       dr = yr;
       di = yi;
       j = 0;

@@ -49,8 +49,13 @@ NM_HD bool delta_xd_steps(const DeviceView& v, DeltaXDState& st, int steps, Esca
       out = {i, (float)sm};
       return true;
     }
-    const XD d2 = xd_add(xd_mul(dr, dr), xd_mul(di, di));
-    if (xd_gt(d2, r2) || j == zlast) {
+    // the rebase test r2 < d2, evaluated only when |Y| is not clearly larger
+    // (larger component of Y at least 4 times delta's: |Y|^2 > 2 |delta|^2)
+    bool rebase = j == zlast;
+    const int32_t ey = yr.e > yi.e ? yr.e : yi.e, ed = dr.e > di.e ? dr.e : di.e;
+    if (!rebase && !(ey >= ed + 2 && (yr.m != 0.0 || yi.m != 0.0)))
+      rebase = xd_gt(xd_add(xd_mul(dr, dr), xd_mul(di, di)), r2);
+    if (rebase) {
       dr = yr;
       di = yi;
       j = 0;

@@ -187,13 +187,14 @@ __global__ void __launch_bounds__(kPersistentThreads) fe_iter_kernel(DeviceView 
   fe_iter_warp(v, b, ctl, chunk);
 }
 
-// The iteration pass with the FP64 rework overlapped: the last warp of every
-// block renders uncertified samples in FP64 (the FP64 pipe is idle under the
-// FP32 iteration) from the start; the other warps iterate in FP32 and, when
-// the FP32 work list is exhausted, join the FP64 side.  Capped at 64
-// registers so that 4 blocks fit on an SM (on the C2 view: 203 ms against
-// 213 ms with two FP64 warps a block and 229 ms uncapped at 3 blocks).
-constexpr int kOverlapWarps = 1;
+// The iteration pass with the FP64 rework overlapped: the last two warps of
+// every block render uncertified samples in FP64 (the FP64 pipe is idle under
+// the FP32 iteration) from the start; the other warps iterate in FP32 and,
+// when the FP32 work list is exhausted, join the FP64 side.  Capped at 64
+// registers so that 4 blocks fit on an SM.  On the C2 view (2.7 % of the
+// samples reworked): 216 ms with two FP64 warps a block, 262 ms with one,
+// 231 ms with three, 273 ms with the rework after the pass.
+constexpr int kOverlapWarps = 2;
 
 // The FP64 side, out of line: its register pressure (the FP64 series front)
 // then stays out of the FP32 iteration's allocation.

@@ -180,12 +180,12 @@ __global__ void __launch_bounds__(kPersistentThreads) batch_list_kernel(BatchGro
 }
 
 // The FE32 iteration of every FE32 frame with the FP64 work overlapped (the
-// FP64 pipe is idle under the FP32 iteration): the last warp of every block
-// renders the double-path frames' samples and then the uncertified FE32
+// FP64 pipe is idle under the FP32 iteration): the last two warps of every
+// block render the double-path frames' samples and then the uncertified FE32
 // samples as they are appended; the other warps iterate in FP32 and, when the
 // FP32 work list is exhausted, join the FP64 side.  Capped at 64 registers so
 // that 4 blocks fit on an SM.
-constexpr int kBatchOverlapWarps = 1;
+constexpr int kBatchOverlapWarps = 2;
 
 // The FP64 side, out of line: its register pressure (the FP64 series front)
 // then stays out of the FP32 iteration's allocation.

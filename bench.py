@@ -348,8 +348,9 @@ def video_views(nframes, nr, nc, w0="4.0", w1="1e-200", n0=1000, n1=500000):
 
 def run_video(args):
     """240 frames of 1280x720 with 2x2 samples (widths 4 -> 1e-200, N 1e3 ->
-    5e5): all frames in one batched CUDA-graph launch (FE32 below the double
-    path's range) against frame-at-a-time plain FP64."""
+    5e5): all frames on the FE32 path in one batched CUDA-graph launch against
+    frame-at-a-time plain FP64 (the reference's double loop on the frames it
+    renders with doubles, the FP64 perturbation path on the others)."""
     import concurrent.futures as cf
     import torch
     import newman_gb300 as nm
@@ -357,12 +358,14 @@ def run_video(args):
     nf, nr, nc, sc = args.frames, 720, 1280, 2
     views = video_views(nf, nr, nc)
 
-    def frame(step, N, deep_path):
+    def frame(step, N, path):
+        # every frame on the FE32 path: the double-loop frames certified
+        # against the double loop, the others against the FP64 path
         m = nm.Mandelbrot(nr, nc)
         m.set_view(CENTER[0], CENTER[1], step, step, N, TOL)
         m.scaleUp(sc)
+        m.set_path(path)
         if not m.useHardware():
-            m.set_path(deep_path)
             m.set_option(nm.OPT_REFERENCE, nm.REFERENCE_CENTER)
         m.precompute()
         return m
@@ -394,8 +397,7 @@ def run_video(args):
     fp_frames = [f.copy() for f in fe_frames]
     fp_ms = 0.0
     for f in fp_frames:
-        if not f.useHardware():
-            f.set_path(nm.PATH_FP64)
+        f.set_path(nm.PATH_REFERENCE if f.useHardware() else nm.PATH_FP64)
         f.upload()
         f.render()  # warm
         f.render()

@@ -31,6 +31,22 @@ namespace {
 
 thread_local std::string g_last_error;
 
+// Precision of the view-center orbit for the FE32 path on a double-loop view:
+// the certificate takes that orbit as exact to the 2^-52 of its FP64 copy.
+constexpr unsigned long kDoubleLoopOrbitBits = 256;
+
+// The FE32 path on a double-loop view certifies against the double loop's own
+// rounding, which grows with the zoom: below a sample step of 2^-33 most
+// samples cannot be certified (measured on the C4 zoom: reworked fraction 7 %
+// at step 6e-10, 24 % at 1e-10, over 90 % below 1e-13), so there the FE32
+// path renders with the double loop directly -- the same escape counts.
+constexpr double kDoubleLoopFe32MinStep = 0x1p-33;
+
+bool double_loop_direct(const nm_handle* h) {
+  return h->path == NM_PATH_FE32 && h->view.use_hardware() &&
+         h->view.step_max() < kDoubleLoopFe32MinStep;
+}
+
 }  // namespace
 
 int nmg::fail(int code, const char* fmt, ...) {
@@ -166,9 +182,13 @@ void set_fe_tables(const nm_handle* h, nmg::DeviceView& v) {
 
 int nmg::prepare_view(nm_handle* h, int r0, int r1, nmg::DeviceView& v, nmg::KernelKind& kind) {
   const int nr = h->view.rows(), nc = h->view.cols();
-  const bool hw = h->view.use_hardware() && h->path == NM_PATH_REFERENCE;
+  const bool hw =
+      h->view.use_hardware() && (h->path == NM_PATH_REFERENCE || double_loop_direct(h));
   if (!hw && !h->precomputed)
     return fail(NM_ERR_STATE, "deep view: nm_precompute must run before rendering");
+  if (!hw && h->od.double_loop && h->path != NM_PATH_FE32)
+    return fail(NM_ERR_STATE, "precomputed for the FE32 path on a double-loop view; "
+                              "nm_precompute again after changing the path");
   if (int rc = ensure_grid(h)) return rc;
   if (int rc = ensure_coords(h)) return rc;
   if (!h->uploaded)
@@ -204,6 +224,7 @@ int nmg::prepare_view(nm_handle* h, int r0, int r1, nmg::DeviceView& v, nmg::Ker
     v.sa_c = h->d_c.p;
     v.sa_min = h->d_sa_min.p;
     set_fe_tables(h, v);
+    v.double_loop = h->od.double_loop ? 1 : 0;
   }
   v.grid = h->grid.p;
   v.smooth64 = h->keep_smooth64 ? h->smooth64.p : nullptr;
@@ -435,7 +456,19 @@ int nm_precompute(nm_handle* h) {
   h->coords_valid = false;
   if (int rc = ensure_coords(h)) return rc;
   h->precomputed = false;
-  if (!h->view.use_hardware() || h->path != NM_PATH_REFERENCE) {
+  if (double_loop_direct(h)) {
+    // rendered by the double loop: nothing to precompute
+  } else if (h->view.use_hardware() && h->path == NM_PATH_FE32) {
+    // the FE32 path on a view the reference renders with its double loop:
+    // the view-center orbit at 256 bits or more, offsets of the loop's start
+    if (h->view.precompute_center_orbit(h->od, kDoubleLoopOrbitBits))
+      return fail(NM_ERR_STATE, "precompute failed");
+    std::vector<double> px(h->coord_re.size()), py(h->coord_im.size());
+    for (size_t c = 0; c < px.size(); c++) px[c] = h->coord_re[c].x;
+    for (size_t r = 0; r < py.size(); r++) py[r] = h->coord_im[r].x;
+    h->view.eps_tables_double_loop(px, py, h->eps_re, h->eps_im);
+    h->precomputed = true;
+  } else if (!h->view.use_hardware() || h->path != NM_PATH_REFERENCE) {
     int threads = h->threads > 0 ? h->threads : (int)std::thread::hardware_concurrency();
     if (h->view.precompute(threads, h->od, h->reference_mode))
       return fail(NM_ERR_STATE, "precompute failed");
@@ -541,8 +574,8 @@ int nm_render_rows(nm_handle* h, int r0, int r1, void* stream_arg) {
     // renders them again, reading the list and its length from the GPU (after
     // an overlapped iteration pass: only the entries it left unclaimed).
     const nmg::RenderCtl re = rework_ctl(h, ctl);
-    int rblocks = h->blocks > 0 ? h->blocks : nmg::persistent_blocks(nmg::KERNEL_DELTA64, h->device);
-    NM_CUDA(nmg::launch_render(nmg::KERNEL_DELTA64, v, re, s, rblocks, h->chunk));
+    int rblocks = h->blocks > 0 ? h->blocks : nmg::persistent_blocks(nmg::KERNEL_REWORK, h->device);
+    NM_CUDA(nmg::launch_render(nmg::KERNEL_REWORK, v, re, s, rblocks, h->chunk));
     NM_CUDA(cudaEventRecord(h->ev[2], s));
   }
   return NM_OK;
@@ -635,13 +668,20 @@ nm_handle* nm_preview(const nm_handle* src, int factor) {
   h->renorm = src->renorm;
   h->reference_mode = src->reference_mode;
   h->fe_overlap = src->fe_overlap;
-  if (src->precomputed && src->reference_mode == nmg::REFERENCE_CENTER) {
+  if (src->precomputed && (src->reference_mode == nmg::REFERENCE_CENTER || src->od.double_loop)) {
     // the orbit at the view center and its series do not depend on the grid:
     // only the per-row / per-column tables are the preview's own
     h->od = src->od;
     if (ensure_coords(h.get()) != NM_OK) return nullptr;
-    h->view.eps_tables(h->od, h->eps_re, h->eps_im);
-    if (!h->od.sa_fp64_ok) h->view.eps_tables_fe(h->eps_re_fe, h->eps_im_fe);
+    if (h->od.double_loop) {
+      std::vector<double> px(h->coord_re.size()), py(h->coord_im.size());
+      for (size_t c = 0; c < px.size(); c++) px[c] = h->coord_re[c].x;
+      for (size_t r = 0; r < py.size(); r++) py[r] = h->coord_im[r].x;
+      h->view.eps_tables_double_loop(px, py, h->eps_re, h->eps_im);
+    } else {
+      h->view.eps_tables(h->od, h->eps_re, h->eps_im);
+      if (!h->od.sa_fp64_ok) h->view.eps_tables_fe(h->eps_re_fe, h->eps_im_fe);
+    }
     h->precomputed = true;
   }
   return h.release();
@@ -837,8 +877,9 @@ void noalloc_fail(const std::string& why) { g_last_error = why; }
 
 // The device view of a handle whose tables are already on the GPU, for the
 // allocation-free entry point (noalloc.cu): only reads the handle.
-int noalloc_view(nm_handle* h, DeviceView& v, int& device, std::string& why) {
-  if (!h->precomputed || !h->uploaded || !h->stream || !h->d_zf.p) {
+int noalloc_view(nm_handle* h, DeviceView& v, int& device, std::string& why, KernelKind& kind) {
+  kind = double_loop_direct(h) ? KERNEL_HW : KERNEL_FE32;
+  if (!h->uploaded || !h->stream || (kind == KERNEL_FE32 && (!h->precomputed || !h->d_zf.p))) {
     why = "the view's tables are not on the GPU: call nm_precompute and nm_upload first";
     return NM_ERR_STATE;
   }
@@ -873,6 +914,7 @@ int noalloc_view(nm_handle* h, DeviceView& v, int& device, std::string& why) {
   v.sa_c = h->d_c.p;
   v.sa_min = h->d_sa_min.p;
   set_fe_tables(h, v);
+  v.double_loop = h->od.double_loop ? 1 : 0;
   device = h->device;
   return NM_OK;
 }

@@ -34,7 +34,9 @@ struct RenderCtl {
   unsigned long long* rework_n;
 };
 
-enum KernelKind { KERNEL_HW = 0, KERNEL_DELTA64 = 1, KERNEL_FE32 = 2 };
+// KERNEL_REWORK: the FE32 path's FP64 rework (the double loop on double-loop
+// views, else the FP64 delta path).
+enum KernelKind { KERNEL_HW = 0, KERNEL_DELTA64 = 1, KERNEL_FE32 = 2, KERNEL_REWORK = 3 };
 
 // Buffers of the FE32 pass pipeline (render_fe32.cu), one record per sample
 // index in tile order.

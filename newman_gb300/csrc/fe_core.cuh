@@ -55,7 +55,9 @@ struct alignas(16) FeState {
   int32_t E;      // 0: unscaled
   int32_t j, i;   // orbit index, iteration count (getIterations' i)
   int32_t certified;
-  int32_t pad_[3];
+  int32_t frame;  // frame of a batch
+  float e64;      // double-loop views: bound on the double loop's own error
+  int32_t pad_;
 };
 
 // Finished sample: escape iteration (N: no escape) and |Y|^2 at the escape.
@@ -74,8 +76,39 @@ __device__ __forceinline__ ZFF fe_load_z(const DeviceView& v, int j) {
   return ZFF{z.x, z.y, z.z, z.w};
 }
 
-// Start state from the FP64 series front (bit-identical to the FP64 path's).
-__device__ __forceinline__ void fe_start(const SeriesFront& f, FeState& st) {
+// The front of a double-loop view (getIterationsHW, mandelbrot.cpp:231-254):
+// the reference's cardioid test, then the perturbation start Y_1 = Z_1 + eps =
+// the double coordinate the loop starts from; no series skip.
+__device__ __forceinline__ bool double_loop_front(const DeviceView& v, int r, int c,
+                                                  SeriesFront& f, EscapeValue& out, double& sm,
+                                                  bool& undecided) {
+  undecided = false;
+  if (v.cardioid_mode == CARDIOID_PER_SAMPLE &&
+      in_cardioid_dd(v.coord_re[c], v.coord_im[r], undecided)) {
+    out = {v.N, 0.0f};
+    sm = 0.0;
+    return true;
+  }
+  f.eps = C64{v.eps_re[c], v.eps_im[r]};
+  f.dfound = f.eps;
+  f.dsize = 1;
+  f.eps_e = 0;
+  f.d_e = 0;
+  return false;
+}
+
+// The front of the FE32 path: the double-loop front or the series front.
+__device__ __forceinline__ bool fe_front(const DeviceView& v, int r, int c, SeriesFront& f,
+                                         EscapeValue& out, double& sm, bool& undecided) {
+  if (v.double_loop) return double_loop_front(v, r, c, f, out, sm, undecided);
+  return series_front_any(v, r, c, f, out, sm, undecided);
+}
+
+// Start state from the front (bit-identical to the FP64 path's).  A
+// double-loop view starts at Z index 1 (Y = the loop's start value) with
+// iteration count 0, so that the escape test after step `it` sees the
+// double loop's z after its step `it`.
+__device__ __forceinline__ void fe_start(const DeviceView& v, const SeriesFront& f, FeState& st) {
   // exponent of the larger of |d[found]| and |eps| (their mantissas carry
   // their own exponents d_e, eps_e in floatexp views)
   const double dm = fmax(fabs(f.dfound.re), fabs(f.dfound.im));
@@ -90,8 +123,11 @@ __device__ __forceinline__ void fe_start(const SeriesFront& f, FeState& st) {
   st.ei = ff_from_double(scalbn(f.eps.im, f.eps_e - E));
   st.err = up_mul(kFeU, up_add(fabsf(st.dr.h), fabsf(st.di.h)));
   st.j = f.dsize;
-  st.i = f.dsize;
+  st.i = v.double_loop ? 0 : f.dsize;
   st.certified = 1;
+  st.frame = 0;
+  st.e64 = 0.0f;
+  st.pad_ = 0;
 }
 
 // sqrt(x) from the hardware reciprocal square root (relative error below
@@ -251,7 +287,13 @@ __device__ __forceinline__ bool fe_scaled_steps(const DeviceView& v, FeState& st
 __device__ __forceinline__ bool fe_advance(const DeviceView& v, FeState& st, int steps,
                                            FeResult& res, unsigned long long& executed,
                                            unsigned long long& rebases) {
-  if (st.E != 0) return fe_scaled_steps(v, st, steps, res, executed, rebases);
+  if (st.E != 0) {
+    if (v.double_loop) {  // a start below 2^-60: left to the double loop
+      st.certified = 0;
+      return true;
+    }
+    return fe_scaled_steps(v, st, steps, res, executed, rebases);
+  }
   const int zlast = v.zlen - 1;
   const int stop = min(v.N, st.i + steps);
   const int start = st.i;
@@ -260,6 +302,8 @@ __device__ __forceinline__ bool fe_advance(const DeviceView& v, FeState& st, int
   const FF er = st.er, ei = st.ei;
   FF dr = st.dr, di = st.di;
   float err = st.err;
+  float e64 = st.e64;
+  const bool dloop = v.double_loop != 0;
   int j = st.j, i = st.i;
   bool certified = st.certified != 0;
   ZFF z = fe_load_z(v, j);
@@ -276,6 +320,7 @@ __device__ __forceinline__ bool fe_advance(const DeviceView& v, FeState& st, int
     const float ym_up = up_fma(0x1p-20f, up_add(zl1, dl1), ym);
     const float loc = up_fma(kFeU, up_fma(up_add(fabsf(tr.h), fabsf(ti.h)), dl1, eps_l1),
                              up_mul(kFeUZ, up_mul(up_fma(2.0f, zl1, dl1), dl1)));
+    const float err_old = err;
     err = up_fma(up_fma(2.0f, ym_up, err), err, loc);  // 2|Y| e + e^2 + local rounding
     FF nr, ni;
     ff_cmul_add(tr, ti, dr, di, er, ei, nr, ni);
@@ -288,7 +333,20 @@ __device__ __forceinline__ bool fe_advance(const DeviceView& v, FeState& st, int
     ym = approx_sqrt(r2);
     const float zn1 = up_add(fabsf(z.hx), fabsf(z.hy)), dn1 = up_add(fabsf(dr.h), fabsf(di.h));
     // error of Y = Z + delta held in float-float (the rebase value)
-    const float yerr = up_add(err, up_fma(kFeUZ, zn1, up_mul(kFeU, up_add(zn1, dn1))));
+    const float yerr_fe = up_add(err, up_fma(kFeUZ, zn1, up_mul(kFeU, up_add(zn1, dn1))));
+    float yerr = yerr_fe;
+    if (dloop) {
+      // The double loop's own distance from exact arithmetic, d' <= (|z| + |w|) d
+      // + its rounding: with |w| <= |Y| + e (the exact orbit) and |z| <= |w| + d,
+      // d' <= (2(|Y| + e) + d) d + 2^-52 (2 |z|^2 + |z'|_1); its bailout test
+      // rounds |z|^2 by 2^-52 more.  The tests below take the sum of both bounds.
+      const float w_old = up_add(ym_up, err_old);
+      const float z_old = up_add(w_old, e64);
+      const float z_new = up_add(up_add(zn1, dn1), up_add(err, e64));
+      const float l64 = up_mul(0x1p-52f, up_fma(up_mul(2.0f, z_old), z_old, z_new));
+      e64 = up_fma(up_fma(2.0f, w_old, e64), e64, l64);
+      yerr = up_add(yerr, up_fma(0x1p-52f, z_new, e64));
+    }
     if (r2 <= lo_band) {
       // |Y| is below the bailout by more than 2^-11 of it; the estimate ym
       // is good to 2^-20 (|Z| + |delta|), so the test is decided unless the
@@ -321,7 +379,7 @@ __device__ __forceinline__ bool fe_advance(const DeviceView& v, FeState& st, int
       const FF nyi = ff_add(FF{z.hy, z.ly}, di);
       dr = nyr;
       di = nyi;
-      err = yerr;
+      err = yerr_fe;
       j = 0;
       z = fe_load_z(v, 0);
       ym = approx_norm(dr.h, di.h);
@@ -332,6 +390,7 @@ __device__ __forceinline__ bool fe_advance(const DeviceView& v, FeState& st, int
   st.dr = dr;
   st.di = di;
   st.err = err;
+  st.e64 = e64;
   st.j = j;
   st.i = i;
   st.certified = certified ? 1 : 0;

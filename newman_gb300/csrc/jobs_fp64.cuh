@@ -68,4 +68,28 @@ struct Delta64Job {
   }
 };
 
+// The FP64 rework of the FE32 path: the double loop on double-loop views (the
+// FE32 path's comparator there), else the FP64 perturbation path.
+struct Fp64AnyJob {
+  union State {
+    HwJob::State hw;
+    Delta64Job::State d;
+  };
+  static constexpr bool kCertifies = false;
+  static constexpr int kCostWeight = kCostFp64Step;
+  static __device__ __forceinline__ bool certified(const State&) { return true; }
+  static __device__ __forceinline__ bool init(const DeviceView& v, int r, int c, State& st,
+                                              EscapeValue& out, double& sm, bool& und) {
+    if (v.double_loop) return HwJob::init(v, r, c, st.hw, out, sm, und);
+    return Delta64Job::init(v, r, c, st.d, out, sm, und);
+  }
+  static __device__ __forceinline__ bool steps(const DeviceView& v, State& st, int n,
+                                               EscapeValue& out, double& sm,
+                                               unsigned long long& executed,
+                                               unsigned long long& rebases) {
+    if (v.double_loop) return HwJob::steps(v, st.hw, n, out, sm, executed, rebases);
+    return Delta64Job::steps(v, st.d, n, out, sm, executed, rebases);
+  }
+};
+
 }  // namespace nmg

@@ -496,6 +496,73 @@ int MPView::precompute(int threads, OrbitData& od, int reference_mode) {
   return 0;
 }
 
+int MPView::precompute_center_orbit(OrbitData& od, unsigned long orbit_bits) {
+  od = OrbitData();
+  od.double_loop = true;
+  od.probe_index = 0;
+  const unsigned long bits = orbit_bits > bits_ ? orbit_bits : bits_;
+  Mpf cr(bits), ci(bits), tmp(bits_), pre(bits_);
+  // pointAt(nr/2 - 1, nc/2) is exactly the center; taken at the view's
+  // precision, then iterated at `bits`
+  coord_re(nc_ / 2, pre, tmp);
+  mpf_set(cr.p(), pre.p());
+  coord_im(nr_ / 2 - 1, pre, tmp);
+  mpf_set(ci.p(), pre.p());
+  x0re_ = cr;
+  x0im_ = ci;
+  StepTemps s(bits);
+  Mpf xr(bits), xi(bits), nxr(bits), nxi(bits), h(64);
+  mpf_set(xr.p(), cr.p());
+  mpf_set(xi.p(), ci.p());
+  od.z.reserve((size_t)std::min(N_, 1 << 20) + 2);
+  od.z.push_back({0.0, 0.0});
+  auto split = [&](mpf_srcptr v, double& hi, double& lo) {
+    hi = mpf_get_d(v);
+    mpf_set_d(h.p(), hi);
+    mpf_sub(s.t3.p(), v, h.p());
+    lo = mpf_get_d(s.t3.p());
+  };
+  bool escaped = false;
+  for (int i = 0;; i++) {
+    D2 hi, lo;
+    split(xr.p(), hi.x, lo.x);
+    split(xi.p(), hi.y, lo.y);
+    od.xhi.push_back(hi);
+    od.xlo.push_back(lo);
+    od.z.push_back(hi);
+    if (i + 1 >= N_) break;
+    square_add(nxr.p(), nxi.p(), xr.p(), xi.p(), cr.p(), ci.p(), s);
+    if (bailed_out(nxr.p(), nxi.p())) {
+      escaped = true;
+      break;
+    }
+    xr.swap(nxr);
+    xi.swap(nxi);
+  }
+  od.xlen = (int)od.xhi.size();
+  if (escaped) od.z.push_back({nxr.d(), nxi.d()});
+  od.sa_fp64_ok = true;
+  return 0;
+}
+
+void MPView::eps_tables_double_loop(const std::vector<double>& px, const std::vector<double>& py,
+                                    std::vector<double>& er, std::vector<double>& ei) const {
+  const unsigned long bits = mpf_get_prec(x0re_.p()) + 64;
+  Mpf t(bits), x(bits);
+  er.resize(px.size());
+  ei.resize(py.size());
+  for (size_t c = 0; c < px.size(); c++) {
+    mpf_set_d(x.p(), px[c]);
+    mpf_sub(t.p(), x.p(), x0re_.p());
+    er[c] = t.d();
+  }
+  for (size_t r = 0; r < py.size(); r++) {
+    mpf_set_d(x.p(), py[r]);
+    mpf_sub(t.p(), x.p(), x0im_.p());
+    ei[r] = t.d();
+  }
+}
+
 bool MPView::view_outside_cardioid() const {
   std::vector<D2> re, im;
   Mpf p(bits_), t(bits_);

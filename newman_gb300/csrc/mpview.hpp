@@ -4,6 +4,9 @@
 // (probe search, reference orbit, series coefficients) that feeds the GPU.
 #pragma once
 
+#include <algorithm>
+#include <cmath>
+
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -60,6 +63,9 @@ struct OrbitData {
   // Floatexp copies (FP64 mantissa, int exponent), used when !sa_fp64_ok:
   std::vector<CFE> a_fe, b_fe, c_fe;
   std::vector<RFE> sa_min_fe;
+  // The orbit alone, for the FE32 path on a view the reference renders with
+  // its double loop (no series: those samples start at iteration 0).
+  bool double_loop = false;
 };
 
 // Where the reference orbit starts.
@@ -85,6 +91,7 @@ class MPView {
   void set_tolerance(double tol) { tol_ = tol; }
 
   bool use_hardware() const;  // mandelbrot.cpp:256-259
+  double step_max() const { return std::max(std::fabs(sre_.d()), std::fabs(sim_.d())); }
   void scale_up(int sc);      // mandelbrot.cpp:334-346 (geometry)
   void scale_down(int sc);    // mandelbrot.cpp:348-360 (geometry)
   void zoom(float scale);     // mandelbrot.cpp:297-302
@@ -111,6 +118,15 @@ class MPView {
   // findProbe + computeSeries (mandelbrot.cpp:73-131), probes on `threads`
   // host threads (or the view center only, REFERENCE_CENTER).  Fills `out`.
   int precompute(int threads, OrbitData& out, int reference_mode = REFERENCE_PROBES);
+
+  // For the FE32 path on a double-loop view: the orbit of the view center at
+  // `orbit_bits` of precision (no series), and per column / row the exact
+  // offset of the double coordinate the double loop starts from,
+  // get_d(get_d(pt) - X[0]) (the inner get_d is computeRow's pt handed to
+  // getIterationsHW, mandelbrot.cpp:242).
+  int precompute_center_orbit(OrbitData& out, unsigned long orbit_bits);
+  void eps_tables_double_loop(const std::vector<double>& px, const std::vector<double>& py,
+                              std::vector<double>& er, std::vector<double>& ei) const;
 
   // Box in which every sample lies is provably outside both the main
   // cardioid and the period-2 disk.

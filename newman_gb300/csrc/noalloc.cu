@@ -18,8 +18,9 @@
 
 namespace nmg {
 // Reads the device tables of a handle that nm_precompute and nm_upload have
-// prepared, without allocating (capi.cpp).
-int noalloc_view(nm_handle* h, DeviceView& v, int& device, std::string& why);
+// prepared, without allocating (capi.cpp).  `kind`: KERNEL_FE32, or KERNEL_HW
+// for a double-loop view that the FE32 path renders with the double loop.
+int noalloc_view(nm_handle* h, DeviceView& v, int& device, std::string& why, KernelKind& kind);
 void noalloc_fail(const std::string& why);
 }  // namespace nmg
 
@@ -75,7 +76,8 @@ extern "C" int nm_render_fe32_noalloc(nm_handle* h, nm_escape_value* out, void* 
   nmg::DeviceView v;
   int device = 0;
   std::string why;
-  if (int rc = nmg::noalloc_view(h, v, device, why)) {
+  nmg::KernelKind kind = nmg::KERNEL_FE32;
+  if (int rc = nmg::noalloc_view(h, v, device, why, kind)) {
     nmg::noalloc_fail("nm_render_fe32_noalloc: " + why);
     return rc;
   }
@@ -93,17 +95,21 @@ extern "C" int nm_render_fe32_noalloc(nm_handle* h, nm_escape_value* out, void* 
   ctl.count = v.total;
   ctl.rework = s ? s->rework : nullptr;
   ctl.rework_n = s ? s->words + kReworkCount : nullptr;
-  if (e == cudaSuccess)
+  if (e == cudaSuccess && kind == nmg::KERNEL_HW) {
+    e = nmg::launch_render(nmg::KERNEL_HW, v, ctl, st,
+                           nmg::persistent_blocks(nmg::KERNEL_HW, device), 32);
+  } else if (e == cudaSuccess) {
     e = nmg::launch_render(nmg::KERNEL_FE32, v, ctl, st,
                            nmg::persistent_blocks(nmg::KERNEL_FE32, device), 16);
-  if (e == cudaSuccess) {
+  }
+  if (e == cudaSuccess && kind == nmg::KERNEL_FE32) {
     nmg::RenderCtl re{};
     re.next = s->words + kNextRework;
     re.stats = s->words + kStatsRework;
     re.list = s->rework;
     re.count_ptr = s->words + kReworkCount;
-    e = nmg::launch_render(nmg::KERNEL_DELTA64, v, re, st,
-                           nmg::persistent_blocks(nmg::KERNEL_DELTA64, device), 32);
+    e = nmg::launch_render(nmg::KERNEL_REWORK, v, re, st,
+                           nmg::persistent_blocks(nmg::KERNEL_REWORK, device), 32);
   }
   if (e != cudaSuccess) {
     nmg::noalloc_fail(std::string("nm_render_fe32_noalloc: ") + cudaGetErrorString(e));

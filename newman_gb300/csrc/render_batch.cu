@@ -10,7 +10,7 @@
 //                                     uncertified samples on the FP64 pipe
 //                                     alongside) -- or batch_iter_kernel
 //                                     without the FP64 side,
-//                 batch_list_kernel<Delta64Job> over the uncertified samples
+//                 batch_list_kernel<Fp64AnyJob> over the uncertified samples
 //                                     (those not yet rendered);
 //   double-path frames (the reference's useHardware views):
 //                 batch_list_kernel<HwJob> over all their samples (those
@@ -70,13 +70,13 @@ __global__ void __launch_bounds__(256) batch_front_kernel(BatchGroup grp, FePass
         EscapeValue out;
         double sm = 0.0;
         bool und = false;
-        if (series_front_any(v, r, c, fr, out, sm, und)) {
+        if (fe_front(v, r, c, fr, out, sm, und)) {
           store_sample(v, r, c, out, sm);
           finished++;
         } else {
           FeState st;
-          fe_start(fr, st);
-          st.pad_[0] = f;
+          fe_start(v, fr, st);
+          st.frame = f;
           b.state[g] = st;
           needs_iteration = true;
         }
@@ -125,7 +125,7 @@ __device__ __forceinline__ void batch_iter_warp(const BatchGroup& grp, const FeP
         } else {
           g = ctl.list[mine];
           st = b.state[g];
-          f = st.pad_[0];
+          f = st.frame;
           active = true;
           exec0 = executed;
         }
@@ -193,7 +193,7 @@ __device__ __noinline__ void batch_fp64_side(const BatchGroup& fe, const BatchGr
                                              const RenderCtl& hw_ctl, const OverlapCtl& o,
                                              unsigned long long producers) {
   if (hw.n > 0) sample_loop<HwJob>(Frames{hw}, hw_ctl, o.chunk);
-  drain_loop<Delta64Job>(Frames{fe}, o.rework, o.fe_warps_done, producers, o.timeouts, o.chunk);
+  drain_loop<Fp64AnyJob>(Frames{fe}, o.rework, o.fe_warps_done, producers, o.timeouts, o.chunk);
 }
 
 __global__ void __launch_bounds__(kPersistentThreads, 4)
@@ -267,8 +267,8 @@ cudaError_t launch_batch(const BatchLaunch& L, cudaStream_t s) {
     else
       batch_iter_kernel<<<blocks_of((const void*)batch_iter_kernel, kPersistentThreads, dev),
                           kPersistentThreads, 0, s>>>(L.fe, L.fe_buf, L.fe_ctl, L.fe_chunk);
-    batch_list_kernel<Delta64Job>
-        <<<blocks_of((const void*)batch_list_kernel<Delta64Job>, kPersistentThreads, dev),
+    batch_list_kernel<Fp64AnyJob>
+        <<<blocks_of((const void*)batch_list_kernel<Fp64AnyJob>, kPersistentThreads, dev),
            kPersistentThreads, 0, s>>>(L.fe, L.rework_ctl, L.chunk);
   }
   // after an overlapped FE32 pass the double-path range is already used up

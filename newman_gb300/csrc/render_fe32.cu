@@ -37,8 +37,8 @@ struct FeJob {
   static __device__ __forceinline__ bool init(const DeviceView& v, int r, int c, State& st,
                                               EscapeValue& out, double& sm, bool& und) {
     SeriesFront f;
-    if (series_front_any(v, r, c, f, out, sm, und)) return true;
-    fe_start(f, st);
+    if (fe_front(v, r, c, f, out, sm, und)) return true;
+    fe_start(v, f, st);
     return false;
   }
   static __device__ __forceinline__ bool steps(const DeviceView& v, State& st, int n,
@@ -82,11 +82,11 @@ __global__ void __launch_bounds__(256) fe_front_kernel(DeviceView v, FePassBuffe
       EscapeValue out;
       double sm = 0.0;
       bool und = false;
-      if (series_front_any(v, r, c, f, out, sm, und)) {
+      if (fe_front(v, r, c, f, out, sm, und)) {
         store_sample(v, r, c, out, sm);
         finished++;
       } else {
-        fe_start(f, b.state[sid]);
+        fe_start(v, f, b.state[sid]);
         needs_iteration = true;
       }
       undecided += und ? 1 : 0;
@@ -200,7 +200,7 @@ constexpr int kOverlapWarps = 2;
 // then stays out of the FP32 iteration's allocation.
 __device__ __noinline__ void overlap_fp64_side(const DeviceView& v, const OverlapCtl& o,
                                                unsigned long long producers) {
-  drain_loop<Delta64Job>(OneView{v}, o.rework, o.fe_warps_done, producers, o.timeouts, o.chunk);
+  drain_loop<Fp64AnyJob>(OneView{v}, o.rework, o.fe_warps_done, producers, o.timeouts, o.chunk);
 }
 
 __global__ void __launch_bounds__(kPersistentThreads, 4) fe_overlap_kernel(

@@ -20,6 +20,11 @@ __global__ void __launch_bounds__(kPersistentThreads) delta64_kernel(DeviceView 
   persistent_loop<Delta64Job>(v, ctl, chunk);
 }
 
+__global__ void __launch_bounds__(kPersistentThreads) rework_kernel(DeviceView v, RenderCtl ctl,
+                                                                      int chunk) {
+  persistent_loop<Fp64AnyJob>(v, ctl, chunk);
+}
+
 cudaError_t launch_fe32(const DeviceView& v, const RenderCtl& ctl, cudaStream_t stream,
                         int blocks, int chunk);
 int fe32_blocks_per_sm();
@@ -34,6 +39,8 @@ int persistent_blocks(KernelKind kind, int device) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, hw_kernel, kPersistentThreads, 0);
   else if (kind == KERNEL_DELTA64)
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, delta64_kernel, kPersistentThreads, 0);
+  else if (kind == KERNEL_REWORK)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rework_kernel, kPersistentThreads, 0);
   else
     per_sm = fe32_blocks_per_sm();
   if (per_sm < 1) per_sm = 1;
@@ -46,6 +53,8 @@ cudaError_t launch_render(KernelKind kind, const DeviceView& v, const RenderCtl&
     hw_kernel<<<blocks, kPersistentThreads, 0, stream>>>(v, ctl, chunk);
   else if (kind == KERNEL_DELTA64)
     delta64_kernel<<<blocks, kPersistentThreads, 0, stream>>>(v, ctl, chunk);
+  else if (kind == KERNEL_REWORK)
+    rework_kernel<<<blocks, kPersistentThreads, 0, stream>>>(v, ctl, chunk);
   else
     return launch_fe32(v, ctl, stream, blocks, chunk);
   return cudaGetLastError();

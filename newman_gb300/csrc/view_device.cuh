@@ -73,6 +73,8 @@ struct DeviceView {
   const double* sa_min;    // [xlen] prefix min of tol |B_i|^2/|C_i|^2
   int32_t sa_scan;         // 1: walk the series term by term (no threshold shortcut)
   int32_t sa_fe;           // 1: eps, series and thresholds in floatexp (tables below)
+  int32_t double_loop;     // 1: FE32 path certified against the double loop (no series;
+                           //    eps = get_d(get_d(pt) - X[0]), orbit at the view center)
   const RFE* eps_re_fe;    // [nc]
   const RFE* eps_im_fe;    // [nr]
   const CFE* sa_a_fe;      // [xlen]

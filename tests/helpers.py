@@ -64,9 +64,10 @@ def zoom_frames(nframes, nr, nc, width0, width1, N0, N1, center=None):
     return out
 
 
-def make_frame(nm, view, sc, deep_path):
-    """A frame handle: the reference's double path where it applies, else
-    `deep_path` with the reference orbit at the view center."""
+def make_frame(nm, view, sc, deep_path, double_loop_path=None):
+    """A frame handle: the reference's double path where it applies (or
+    `double_loop_path` there, when given), else `deep_path` with the reference
+    orbit at the view center."""
     m = nm.Mandelbrot(view["nr"], view["nc"])
     m.set_view(view["cre"], view["cim"], view["step"], view["step"], view["N"], view["tol"])
     if sc > 1:
@@ -74,6 +75,8 @@ def make_frame(nm, view, sc, deep_path):
     if not m.useHardware():
         m.set_path(deep_path)
         m.set_option(nm.OPT_REFERENCE, nm.REFERENCE_CENTER)
+    elif double_loop_path is not None:
+        m.set_path(double_loop_path)
     return m
 
 

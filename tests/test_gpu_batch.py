@@ -92,3 +92,29 @@ def test_batch_overlap_matches_separate_launches(nm, video):
         out.append(batch.frames_out())
     for a, b in zip(*out):
         assert np.array_equal(a, b)
+
+
+def test_batch_with_fe32_double_loop_frames(nm):
+    """All frames on the FE32 path, the double-loop frames included: the batch
+    gives what rendering each frame alone gives, and the double-loop frames'
+    escape counts are the double loop's."""
+    views = zoom_frames(8, 48, 64, "4.0", "1e-40", 500, 8000)
+    frames = [make_frame(nm, v, 2, nm.PATH_FE32, nm.PATH_FE32) for v in views]
+    for f in frames:
+        f.precompute()
+    assert any(f.useHardware() for f in frames)
+    batch = nm.Batch(sc=2)
+    for f in frames:
+        batch.add(f)
+    batch.render()
+    got = batch.frames_out()
+    assert batch.stat(nm.STAT_WAIT_TIMEOUTS) == 0
+    for v, f, g in zip(views, frames, got):
+        alone = make_frame(nm, v, 2, nm.PATH_FE32, nm.PATH_FE32)
+        alone.precompute()
+        alone.render()
+        assert np.array_equal(g["iterations"], alone.reduce(2)["iterations"])
+        if f.useHardware():
+            dl = make_frame(nm, v, 2, nm.PATH_FE32)
+            dl.render()
+            assert (dl.grid()["iterations"] == alone.grid()["iterations"]).mean() >= 0.9999

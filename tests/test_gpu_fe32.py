@@ -7,7 +7,7 @@ FP64 kernel), on the full C2 frame and on small views.
 import numpy as np
 import pytest
 
-from helpers import C2, setup_gpu, shrink
+from helpers import C1, C2, setup_gpu, shrink, step_for
 
 pytestmark = pytest.mark.gpu
 
@@ -20,8 +20,13 @@ def nm():
 
 
 def render_pair(nm, view):
+    """The FE32 path and its comparator: the plain FP64 path, or on a view the
+    reference renders with its double loop, that loop."""
     a = setup_gpu(nm, view, path=nm.PATH_FP64)
-    a.precompute()
+    if a.useHardware():
+        a.set_path(nm.PATH_REFERENCE)
+    else:
+        a.precompute()
     a.render()
     b = setup_gpu(nm, view, path=nm.PATH_FE32)
     b.precompute()
@@ -61,7 +66,7 @@ def test_fe32_counts_every_sample(nm):
 def test_overlapped_rework_gives_the_same_grid(nm):
     """The FP64 rework inside the iteration pass (as uncertified samples
     appear) gives the grid that the rework after the pass gives."""
-    v = shrink(C2, 96, 160, N=20000)
+    v = dict(shrink(C2, 96, 160, N=20000), step=step_for("1e-14", 160))  # below the double loop
     out = []
     for overlap in (0, 1):
         m = setup_gpu(nm, v, path=nm.PATH_FE32)
@@ -75,3 +80,28 @@ def test_overlapped_rework_gives_the_same_grid(nm):
     assert n0 == n1 and n0 > 0
     assert np.array_equal(g0, g1)
     assert np.array_equal(s0, s1)
+
+
+@pytest.mark.parametrize("view", [
+    dict(C1),  # 640x480, width 3, N 1024
+    dict(nr=192, nc=256, sc=1, cre=C2["cre"], cim=C2["cim"], step="2e-10", N=20000, tol=1e-10),
+    dict(nr=32, nc=48, sc=1, cre="-0.1225", cim="0.7449", step="0.004", N=100000, tol=1e-10),
+], ids=["C1", "seahorse-5e-8", "period3-bulb"])
+def test_fe32_on_double_loop_views_matches_the_double_loop(nm, view):
+    """Views the reference renders with its double loop: the FE32 path
+    (perturbation from a 256-bit view-center orbit, certified against the
+    double loop's own rounding as well) gives the double loop's escape
+    counts; uncertified samples are rendered by the double loop itself."""
+    ref = setup_gpu(nm, view)
+    assert ref.useHardware()
+    ref.render()
+    fe = setup_gpu(nm, view, path=nm.PATH_FE32)
+    fe.precompute()
+    fe.render()
+    a, b = ref.grid(), fe.grid()
+    same = a["iterations"] == b["iterations"]
+    print("exact %.6f rework %d" % (same.mean(), fe.stat(nm.STAT_FP64_REWORK)))
+    assert same.mean() >= 0.9999
+    assert fe.stat(nm.STAT_SAMPLES) == fe.rows() * fe.cols()
+    d = np.abs(ref.smoothing64()[same] - fe.smoothing64()[same])
+    assert d.size == 0 or np.median(d) < 1e-6

@@ -16,7 +16,7 @@ import ctypes
 import numpy as np
 import pytest
 
-from helpers import C2, setup_gpu, shrink
+from helpers import C2, setup_gpu, shrink, step_for
 
 pytestmark = pytest.mark.gpu
 
@@ -30,7 +30,8 @@ def nm():
 
 def test_noalloc_matches_allocating_render(nm):
     torch = pytest.importorskip("torch")
-    view = shrink(C2, 135, 240, N=20000)  # 540 x 960 samples
+    # 540 x 960 samples at width 1e-14: a view below the double loop's range
+    view = dict(shrink(C2, 135, 240, N=20000), step=step_for("1e-14", 240))
     m = setup_gpu(nm, view, path=nm.PATH_FE32, keep64=False)
     m.precompute()
     m.upload()

@@ -68,7 +68,9 @@ enum nm_option {
   NM_OPT_BATCH_GRAPH = 9, /* batches: 1 replay one captured CUDA graph (default), 0 launch */
   NM_OPT_FE32_OVERLAP = 10, /* FE32 passes: 1 render the uncertified samples in FP64 inside
                               the iteration pass, as they appear (default); 0 after it */
-  NM_OPT_LOG_TILE_COSTS = 11 /* 1: whole-grid renders log every tile's work (nm_get_tile_costs) */
+  NM_OPT_LOG_TILE_COSTS = 11, /* 1: whole-grid renders log every tile's work (nm_get_tile_costs) */
+  NM_OPT_BATCH_FP64_WARPS = 12 /* batches: warps of 8 a block on the FP64 side of the FE32 pass
+                                  (2, 4 or 6; 0 = 4 with double-loop frames, else 2) */
 };
 
 enum nm_stat {
@@ -214,14 +216,15 @@ nm_batch* nm_batch_create(int sc);
 void nm_batch_destroy(nm_batch* b);
 int nm_batch_add(nm_batch* b, nm_handle* frame);
 /* NM_OPT_TILE_W, NM_OPT_TILE_H, NM_OPT_CHUNK, NM_OPT_RENORM, NM_OPT_BATCH_GRAPH,
-   NM_OPT_FE32_OVERLAP */
+   NM_OPT_FE32_OVERLAP, NM_OPT_BATCH_FP64_WARPS */
 int nm_batch_set_option(nm_batch* b, int option, long long value);
 int nm_batch_render(nm_batch* b);
 /* NM_STAT_EXECUTED_ITERS, NM_STAT_SAMPLES, NM_STAT_FP64_REWORK, NM_STAT_KERNEL_NS */
 int nm_batch_get_stat(nm_batch* b, int stat, long long* value);
 int nm_batch_frames(nm_batch* b, nm_escape_value* host_out);
 /* Times every tile shape (8x8 .. 64x64) and FE32 renormalisation interval
-   (8 .. 256) on every stride-th frame and keeps the fastest. */
+   (8 .. 256) on every stride-th frame and keeps the fastest, then the FP64
+   side's share of the FE32 pass (NM_OPT_BATCH_FP64_WARPS 2, 4, 6). */
 int nm_batch_autotune(nm_batch* b, int stride, int* tile_w, int* tile_h, int* renorm);
 
 /* Render the handle's view on the FP32-floatexp path into device memory the

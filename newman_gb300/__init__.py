@@ -21,7 +21,7 @@ NM_OK, NM_ERR_ARG, NM_ERR_PARSE, NM_ERR_STATE, NM_ERR_CUDA, NM_ERR_CANCELLED, NM
 PATH_REFERENCE, PATH_FP64, PATH_FE32 = 0, 1, 2
 OPT_TILE_W, OPT_TILE_H, OPT_CHUNK, OPT_KEEP_SMOOTH64, OPT_THREADS, OPT_BLOCKS, OPT_RENORM, \
     OPT_FE32_SINGLE_PASS, OPT_REFERENCE, OPT_BATCH_GRAPH, OPT_FE32_OVERLAP, \
-    OPT_LOG_TILE_COSTS = range(12)
+    OPT_LOG_TILE_COSTS, OPT_BATCH_FP64_WARPS = range(13)
 REFERENCE_PROBES, REFERENCE_CENTER = 0, 1
 STAT_CARDIOID_UNDECIDED, STAT_EXECUTED_ITERS, STAT_SAMPLES, STAT_REBASES, STAT_FP64_REWORK, \
     STAT_WAIT_TIMEOUTS = range(6)

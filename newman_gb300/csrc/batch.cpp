@@ -20,6 +20,7 @@ struct nm_batch {
   int tile_w = 16, tile_h = 16, chunk = 32, fe_chunk = 32;
   bool use_graph = true;
   bool overlap = true;  // FP64 work inside the FE32 iteration pass
+  int fp64_warps = 0;   // of 8 a block in that pass; 0: chosen from the batch
 
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -177,6 +178,7 @@ int build(nm_batch* b) {
   L.fe_chunk = b->fe_chunk;
   L.chunk = b->chunk;
   L.overlap = b->overlap;
+  L.fp64_warps = b->fp64_warps;
   L.overlap_ctl.rework = L.rework_ctl;
   L.overlap_ctl.fe_warps_done = w + kFeWarpsDone;
   L.overlap_ctl.timeouts = w + kFeStats + nmg::STAT_WAIT_TIMEOUTS;
@@ -265,6 +267,11 @@ int nm_batch_set_option(nm_batch* b, int opt, long long value) {
     case NM_OPT_FE32_OVERLAP:
       b->overlap = value != 0;
       break;
+    case NM_OPT_BATCH_FP64_WARPS:
+      if (value != 0 && value != 2 && value != 4 && value != 6)
+        return fail(NM_ERR_ARG, "FP64 warps a block %lld (0, 2, 4 or 6)", value);
+      b->fp64_warps = (int)value;
+      break;
     default:
       return fail(NM_ERR_ARG, "option %d does not apply to a batch", opt);
   }
@@ -343,6 +350,7 @@ int nm_batch_autotune(nm_batch* b, int stride, int* tile_w, int* tile_h, int* re
   sub.use_graph = b->use_graph;
   sub.overlap = b->overlap;
   sub.chunk = b->chunk;
+  sub.fp64_warps = b->fp64_warps;
   for (size_t k = 0; k < b->frames.size(); k += (size_t)stride) sub.frames.push_back(b->frames[k]);
   static const int tiles[][2] = {{8, 8}, {16, 16}, {32, 8}, {32, 32}, {64, 16}, {64, 64}};
   static const int renorms[] = {8, 16, 32, 64, 128, 256};
@@ -369,9 +377,34 @@ int nm_batch_autotune(nm_batch* b, int stride, int* tile_w, int* tile_h, int* re
         br = rn;
       }
     }
+  // then the FP64 side's share of each block, at the chosen tiles
+  int bfw = b->fp64_warps;
+  if (b->overlap) {
+    sub.tile_w = bw;
+    sub.tile_h = bh;
+    sub.fe_chunk = br;
+    float best_w = 1e30f;
+    for (int fw : {2, 4, 6}) {
+      sub.fp64_warps = fw;
+      sub.invalidate();
+      if (int rc = nm_batch_render(&sub)) return rc;
+      float ms = 0.f;
+      for (int rep = 0; rep < 2; rep++) {
+        if (int rc = nm_batch_render(&sub)) return rc;
+        float m = 0.f;
+        NM_CUDA(cudaEventElapsedTime(&m, sub.ev0, sub.ev1));
+        ms += m;
+      }
+      if (ms < best_w) {
+        best_w = ms;
+        bfw = fw;
+      }
+    }
+  }
   b->tile_w = bw;
   b->tile_h = bh;
   b->fe_chunk = br;
+  b->fp64_warps = bfw;
   b->invalidate();
   // frames were prepared with the sub-batch's last tile shape: rebuild later
   for (nm_handle* h : b->frames) {

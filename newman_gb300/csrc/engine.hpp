@@ -94,6 +94,7 @@ struct BatchLaunch {
   FePassBuffers fe_buf;
   RenderCtl fe_ctl, rework_ctl, hw_ctl, fp64_ctl;
   bool overlap;             // FP64 work inside the FE32 iteration pass
+  int fp64_warps;           // FP64 warps of 8 a block in that pass (0: by the batch)
   OverlapCtl overlap_ctl;   // its rework side (= rework_ctl) and counters
   int fe_chunk, chunk;
   const ReduceJob* reduce;  // [nreduce], device memory

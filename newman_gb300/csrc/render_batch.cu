@@ -180,12 +180,13 @@ __global__ void __launch_bounds__(kPersistentThreads) batch_list_kernel(BatchGro
 }
 
 // The FE32 iteration of every FE32 frame with the FP64 work overlapped (the
-// FP64 pipe is idle under the FP32 iteration): the last two warps of every
-// block render the double-path frames' samples and then the uncertified FE32
-// samples as they are appended; the other warps iterate in FP32 and, when the
-// FP32 work list is exhausted, join the FP64 side.  Capped at 64 registers so
-// that 4 blocks fit on an SM.
-constexpr int kBatchOverlapWarps = 2;
+// FP64 pipe is idle under the FP32 iteration): the last kFp64Warps warps of
+// every block render the double-path frames' samples and then the
+// uncertified FE32 samples as they are appended; the other warps iterate in
+// FP32 and, when the FP32 work list is exhausted, join the FP64 side.  Capped
+// at 64 registers so that 4 blocks fit on an SM.  The split follows the
+// batch's FP64 work: on the 240-frame C4 zoom (7 double-loop frames) 4 FP64
+// warps of 8 give 1,819 ms, 6 give 1,862 ms, 2 give 2,030 ms (two runs each).
 
 // The FP64 side, out of line: its register pressure (the FP64 series front)
 // then stays out of the FP32 iteration's allocation.
@@ -196,11 +197,12 @@ __device__ __noinline__ void batch_fp64_side(const BatchGroup& fe, const BatchGr
   drain_loop<Fp64AnyJob>(Frames{fe}, o.rework, o.fe_warps_done, producers, o.timeouts, o.chunk);
 }
 
+template <int kFp64Warps>
 __global__ void __launch_bounds__(kPersistentThreads, 4)
     batch_overlap_kernel(BatchGroup fe, FePassBuffers b, RenderCtl fe_ctl, BatchGroup hw,
                          RenderCtl hw_ctl, OverlapCtl o, int chunk) {
   const int warp = threadIdx.x >> 5;
-  const int fe_warps = kPersistentThreads / 32 - kBatchOverlapWarps;
+  const int fe_warps = kPersistentThreads / 32 - kFp64Warps;
   if (warp < fe_warps) {
     batch_iter_warp(fe, b, fe_ctl, chunk);
     producer_warp_done(o.fe_warps_done);
@@ -246,6 +248,26 @@ int blocks_of(const void* kernel, int threads, int device) {
   return sms * (per_sm < 1 ? 1 : per_sm);
 }
 
+template <int kFp64Warps>
+void launch_overlap_with(const BatchLaunch& L, cudaStream_t s) {
+  batch_overlap_kernel<kFp64Warps>
+      <<<blocks_of((const void*)batch_overlap_kernel<kFp64Warps>, kPersistentThreads, L.device),
+         kPersistentThreads, 0, s>>>(L.fe, L.fe_buf, L.fe_ctl, L.hw, L.hw_ctl, L.overlap_ctl,
+                                     L.fe_chunk);
+}
+
+// FP64 warps a block: as set, else 4 when the batch has double-loop frames
+// (their FP64 work dominates), else 2 (the FP64 rework alone).
+void launch_overlap(const BatchLaunch& L, cudaStream_t s) {
+  const int w = L.fp64_warps > 0 ? L.fp64_warps : (L.hw.n > 0 && L.hw.total > 0 ? 4 : 2);
+  if (w <= 2)
+    launch_overlap_with<2>(L, s);
+  else if (w <= 4)
+    launch_overlap_with<4>(L, s);
+  else
+    launch_overlap_with<6>(L, s);
+}
+
 }  // namespace
 
 cudaError_t launch_batch(const BatchLaunch& L, cudaStream_t s) {
@@ -260,10 +282,7 @@ cudaError_t launch_batch(const BatchLaunch& L, cudaStream_t s) {
     batch_front_kernel<<<blocks_of((const void*)batch_front_kernel, 256, dev), 256, 0, s>>>(
         L.fe, L.fe_buf, L.fe_ctl.stats);
     if (L.overlap)
-      batch_overlap_kernel<<<blocks_of((const void*)batch_overlap_kernel, kPersistentThreads,
-                                       dev),
-                             kPersistentThreads, 0, s>>>(L.fe, L.fe_buf, L.fe_ctl, L.hw,
-                                                         L.hw_ctl, L.overlap_ctl, L.fe_chunk);
+      launch_overlap(L, s);
     else
       batch_iter_kernel<<<blocks_of((const void*)batch_iter_kernel, kPersistentThreads, dev),
                           kPersistentThreads, 0, s>>>(L.fe, L.fe_buf, L.fe_ctl, L.fe_chunk);

@@ -248,6 +248,7 @@ def run_ours(args):
     eff_iters = int(g["iterations"].astype(np.int64).sum())
     executed = m.stat(nm.STAT_EXECUTED_ITERS)
     rework = m.stat(nm.STAT_FP64_REWORK)
+    front_fp64 = m.stat(nm.STAT_FRONT_FP64)
     k_main_ms = m.stat(nm.STAT_KERNEL_NS) * 1e-6
     k_rework_ms = m.stat(nm.STAT_REWORK_KERNEL_NS) * 1e-6
     k_iter_ms = m.stat(nm.STAT_ITER_KERNEL_NS) * 1e-6
@@ -301,6 +302,7 @@ def run_ours(args):
             "path": args.path,
             "exact_iter_fraction_vs_fp64": exact, "exact_iter_fraction_reduced_px": exact_px,
             "max_dsmooth_exact_samples": max_dsmooth_exact,
+            "fp64_front_fraction": front_fp64 / float(NR * NC * SC * SC),
             "fp64_rework_fraction": rework / float(NR * NC * SC * SC),
             "fp64_path": None if fp64_ms is None else {
                 "ms_per_step": fp64_ms, "value": eff_iters / (fp64_ms * 1e-3),
@@ -484,6 +486,7 @@ def run_deep(args):
     eff = int(g.astype(np.int64).sum())
     executed = m.stat(nm.STAT_EXECUTED_ITERS)
     rework = m.stat(nm.STAT_FP64_REWORK)
+    front_fp64 = m.stat(nm.STAT_FRONT_FP64)
     # the plain FP64 path over rows [r0, r1) of the same view and orbit
     band = max(1, nr // args.deep_band)
     r0 = (nr - band) // 2
@@ -511,7 +514,7 @@ def run_deep(args):
                    "reference": "orbit at the view center, floatexp series"},
         "orbit_length": m.stat(nm.STAT_ORBIT_LENGTH), "precompute_s": precompute_s,
         "executed_iters_per_step": executed, "effective_iters_per_step": eff,
-        "fp64_rework_samples": rework, "max_escape": int(g[g < N].max()) if (g < N).any() else None,
+        "fp64_rework_samples": rework, "fp64_front_samples": front_fp64, "max_escape": int(g[g < N].max()) if (g < N).any() else None,
         "interior_fraction": float((g == N).mean()),
         "fp64_band": {"rows": [r0, r0 + band], "ms": fp_ms, "value": fp_rate,
                       "unit": "pixel-iters/s", "exact_iter_fraction_vs_fe32": exact},

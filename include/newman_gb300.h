@@ -80,6 +80,7 @@ enum nm_stat {
   NM_STAT_REBASES = 3,            /* perturbation rebases in the last render */
   NM_STAT_FP64_REWORK = 4,        /* FE32 samples not certified, re-rendered in FP64 */
   NM_STAT_WAIT_TIMEOUTS = 5,      /* overlapped FP64 rework: bounded waits that ran out (0) */
+  NM_STAT_FRONT_FP64 = 6,         /* FE32 samples whose series front fell back to FP64 */
   NM_STAT_ORBIT_LENGTH = 16,      /* X.size() of the last precompute */
   NM_STAT_PROBE_INDEX = 17,       /* winning probe of findProbe */
   NM_STAT_PRECISION_BITS = 18,    /* arbitrary precision of the view */

@@ -24,7 +24,7 @@ OPT_TILE_W, OPT_TILE_H, OPT_CHUNK, OPT_KEEP_SMOOTH64, OPT_THREADS, OPT_BLOCKS, O
     OPT_LOG_TILE_COSTS, OPT_BATCH_FP64_WARPS = range(13)
 REFERENCE_PROBES, REFERENCE_CENTER = 0, 1
 STAT_CARDIOID_UNDECIDED, STAT_EXECUTED_ITERS, STAT_SAMPLES, STAT_REBASES, STAT_FP64_REWORK, \
-    STAT_WAIT_TIMEOUTS = range(6)
+    STAT_WAIT_TIMEOUTS, STAT_FRONT_FP64 = range(7)
 STAT_ORBIT_LENGTH, STAT_PROBE_INDEX, STAT_PRECISION_BITS, STAT_PRECOMPUTE_US = 16, 17, 18, 19
 STAT_KERNEL_NS, STAT_REWORK_KERNEL_NS, STAT_ITER_KERNEL_NS = 20, 21, 22
 

@@ -144,6 +144,14 @@ int do_upload(nm_handle* h) {
     if ((rc = upload(h->d_b, cv(h->od.b), h->stream))) return rc;
     if ((rc = upload(h->d_c, cv(h->od.c), h->stream))) return rc;
     if ((rc = upload(h->d_sa_min, h->od.sa_min, h->stream))) return rc;
+    if (!h->od.double_loop) {
+      if ((rc = upload(h->d_eps32_re, h->eps32_re, h->stream))) return rc;
+      if ((rc = upload(h->d_eps32_im, h->eps32_im, h->stream))) return rc;
+      if ((rc = upload(h->d_a32, h->a32, h->stream))) return rc;
+      if ((rc = upload(h->d_b32, h->b32, h->stream))) return rc;
+      if ((rc = upload(h->d_c32, h->c32, h->stream))) return rc;
+      if ((rc = upload(h->d_sa_min32, h->sa_min32, h->stream))) return rc;
+    }
     if (!h->od.sa_fp64_ok) {
       if ((rc = upload(h->d_eps_re_fe, h->eps_re_fe, h->stream))) return rc;
       if ((rc = upload(h->d_eps_im_fe, h->eps_im_fe, h->stream))) return rc;
@@ -160,6 +168,70 @@ int do_upload(nm_handle* h) {
   return NM_OK;
 }
 
+// ---- tables of the FP32 series front ------------------------------------
+nmg::FFE ffe_of(double m, int e) {
+  if (m == 0.0 || !std::isfinite(m)) return {0.0f, 0.0f, 0, 0};
+  const int k = std::ilogb(m);
+  const double x = std::scalbn(m, -k);  // [1, 2)
+  const float hi = (float)x;
+  return {hi, (float)(x - (double)hi), e + k, 0};
+}
+nmg::CFFE cffe_of(double re, double im, int e) {
+  const double mx = std::max(std::fabs(re), std::fabs(im));
+  if (mx == 0.0 || !std::isfinite(mx)) return {0.0f, 0.0f, 0.0f, 0.0f, 0, {0, 0, 0}};
+  const int k = std::ilogb(mx);
+  const double xr = std::scalbn(re, -k), xi = std::scalbn(im, -k);
+  const float rh = (float)xr, ih = (float)xi;
+  return {rh, (float)(xr - (double)rh), ih, (float)(xi - (double)ih), e + k, {0, 0, 0}};
+}
+nmg::TFE tfe_of(double m, int e) {
+  if (std::isinf(m) && m > 0.0) return {1.0f, nmg::kTfeInf};
+  if (!(m > 0.0)) return {0.0f, nmg::kTfeZero};  // 0 or NaN: below every threshold
+  int k = std::ilogb(m);
+  float x = (float)std::scalbn(m, -k);
+  if (x >= 2.0f) {
+    x *= 0.5f;
+    k++;
+  }
+  return {x, e + k};
+}
+
+// The series front's values in float-float with int exponents: eps per
+// column / row, A, B, C and the thresholds per index.  Deep views only.
+void build_front32_tables(nm_handle* h) {
+  const nmg::OrbitData& od = h->od;
+  const int n = od.xlen;
+  h->a32.resize(n);
+  h->b32.resize(n);
+  h->c32.resize(n);
+  h->sa_min32.resize(n);
+  if (od.sa_fp64_ok) {
+    for (int i = 0; i < n; i++) {
+      h->a32[i] = cffe_of(od.a[i].x, od.a[i].y, 0);
+      h->b32[i] = cffe_of(od.b[i].x, od.b[i].y, 0);
+      h->c32[i] = cffe_of(od.c[i].x, od.c[i].y, 0);
+      h->sa_min32[i] = tfe_of(od.sa_min[i], 0);
+    }
+    h->eps32_re.resize(h->eps_re.size());
+    h->eps32_im.resize(h->eps_im.size());
+    for (size_t c = 0; c < h->eps_re.size(); c++) h->eps32_re[c] = ffe_of(h->eps_re[c], 0);
+    for (size_t r = 0; r < h->eps_im.size(); r++) h->eps32_im[r] = ffe_of(h->eps_im[r], 0);
+  } else {
+    for (int i = 0; i < n; i++) {
+      h->a32[i] = cffe_of(od.a_fe[i].re, od.a_fe[i].im, od.a_fe[i].e);
+      h->b32[i] = cffe_of(od.b_fe[i].re, od.b_fe[i].im, od.b_fe[i].e);
+      h->c32[i] = cffe_of(od.c_fe[i].re, od.c_fe[i].im, od.c_fe[i].e);
+      h->sa_min32[i] = tfe_of(od.sa_min_fe[i].m, od.sa_min_fe[i].e);
+    }
+    h->eps32_re.resize(h->eps_re_fe.size());
+    h->eps32_im.resize(h->eps_im_fe.size());
+    for (size_t c = 0; c < h->eps_re_fe.size(); c++)
+      h->eps32_re[c] = ffe_of(h->eps_re_fe[c].m, h->eps_re_fe[c].e);
+    for (size_t r = 0; r < h->eps_im_fe.size(); r++)
+      h->eps32_im[r] = ffe_of(h->eps_im_fe[r].m, h->eps_im_fe[r].e);
+  }
+}
+
 int check_handle(const nm_handle* h) {
   if (!h) return fail(NM_ERR_ARG, "null handle");
   return NM_OK;
@@ -168,6 +240,14 @@ int check_handle(const nm_handle* h) {
 // Views outside the FP64 range run their series front in floatexp.
 void set_fe_tables(const nm_handle* h, nmg::DeviceView& v) {
   v.sa_scan = 0;
+  if (!h->od.double_loop && !h->a32.empty()) {
+    v.eps32_re = h->d_eps32_re.p;
+    v.eps32_im = h->d_eps32_im.p;
+    v.sa_a32 = h->d_a32.p;
+    v.sa_b32 = h->d_b32.p;
+    v.sa_c32 = h->d_c32.p;
+    v.sa_min32 = h->d_sa_min32.p;
+  }
   v.sa_fe = h->od.sa_fp64_ok ? 0 : 1;
   if (!v.sa_fe) return;
   v.eps_re_fe = h->d_eps_re_fe.p;
@@ -278,6 +358,12 @@ nm_handle* nm_copy(const nm_handle* src) {
   h->eps_im = src->eps_im;
   h->eps_re_fe = src->eps_re_fe;
   h->eps_im_fe = src->eps_im_fe;
+  h->eps32_re = src->eps32_re;
+  h->eps32_im = src->eps32_im;
+  h->a32 = src->a32;
+  h->b32 = src->b32;
+  h->c32 = src->c32;
+  h->sa_min32 = src->sa_min32;
   h->reference_mode = src->reference_mode;
   h->fe_single_pass = src->fe_single_pass;
   h->fe_overlap = src->fe_overlap;
@@ -474,6 +560,7 @@ int nm_precompute(nm_handle* h) {
       return fail(NM_ERR_STATE, "precompute failed");
     h->view.eps_tables(h->od, h->eps_re, h->eps_im);
     if (!h->od.sa_fp64_ok) h->view.eps_tables_fe(h->eps_re_fe, h->eps_im_fe);
+    build_front32_tables(h);
     h->precomputed = true;
   }
   h->precompute_us =
@@ -681,6 +768,7 @@ nm_handle* nm_preview(const nm_handle* src, int factor) {
     } else {
       h->view.eps_tables(h->od, h->eps_re, h->eps_im);
       if (!h->od.sa_fp64_ok) h->view.eps_tables_fe(h->eps_re_fe, h->eps_im_fe);
+      build_front32_tables(h.get());
     }
     h->precomputed = true;
   }

@@ -14,6 +14,7 @@ enum StatIndex {
   STAT_REBASES = 3,             // rebases of the perturbation delta
   STAT_REWORK = 4,              // samples the FE32 kernel handed to the FP64 kernel
   STAT_WAIT_TIMEOUTS = 5,       // bounded waits of the overlapped rework that ran out
+  STAT_FRONT_FP64 = 6,          // FE32 samples whose series front needed FP64
   STAT_COUNT = 8
 };
 

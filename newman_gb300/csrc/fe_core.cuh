@@ -130,6 +130,166 @@ __device__ __forceinline__ void fe_start(const DeviceView& v, const SeriesFront&
   st.pad_ = 0;
 }
 
+// ---- the series front on the FP32 pipe ---------------------------------------
+//
+// The FP64 front (pixel_fp64.cuh, pixel_fe64.cuh) decides two things that the
+// FE32 path must reproduce exactly -- the series stop index and whether the
+// sample escapes before it -- and computes d[found], which the FE32 path only
+// needs to within its error bound.  Here:
+//   stop index: the first i with T_i < u, u = |eps3|^2/|eps2|^2 = |eps|^2 in
+//     exact arithmetic; the FP64 front's u is within 2^-40 of |eps|^2 and its
+//     own thresholds are exact there, so where no threshold T_i lies within
+//     2^-18 of the FP32 |eps|^2 (good to 2^-22) both fronts stop at the same i;
+//   escape before the stop: impossible when |X[found]|_1 + |d|_1 < 1023.5;
+//   d[found] = A eps + B eps^2 + C eps^3 in float-float with exponents, within
+//     2^-40 (|A eps| + |B eps^2| + |C eps^3|) of the FP64 front's value, which
+//     goes into the starting error bound.
+// Any other sample (a threshold in the band, an orbit element near the
+// bailout) returns kFront32Undecided and takes the FP64 front.
+
+constexpr int kFront32Ready = 0, kFront32Finished = 1, kFront32Undecided = 2;
+
+struct CFF {  // ((re) + i (im)) * 2^e, float-float mantissas
+  FF re, im;
+  int e;
+};
+
+__device__ __forceinline__ FF ffe_scaled(float h, float l, int d) {
+  if (h == 0.0f || d < -140) return FF{0.0f, 0.0f};
+  return ff_scale(FF{h, l}, d);
+}
+__device__ __forceinline__ float cff_l1(const CFF& a) { return fabsf(a.re.h) + fabsf(a.im.h); }
+__device__ __forceinline__ CFF cff_mul(const CFF& a, const CFF& b) {
+  CFF r;
+  ff_cmul_add(a.re, a.im, b.re, b.im, FF{0.0f, 0.0f}, FF{0.0f, 0.0f}, r.re, r.im);
+  r.e = a.e + b.e;
+  return r;
+}
+__device__ __forceinline__ CFF cff_of(const CFFE& x) {
+  return CFF{FF{x.rh, x.rl}, FF{x.ih, x.il}, x.e};
+}
+__device__ __forceinline__ bool tfe_less(TFE a, TFE b) {
+  return a.e < b.e || (a.e == b.e && a.m < b.m);
+}
+__device__ __forceinline__ int first_below32(const TFE* t, int lo, int hi, TFE x) {
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (tfe_less(t[mid], x))
+      hi = mid;
+    else
+      lo = mid + 1;
+  }
+  return lo;
+}
+__device__ __forceinline__ TFE tfe_norm(float m, int e) {
+  if (!(m > 0.0f)) return TFE{0.0f, kTfeZero};
+  const int k = ilogbf(m);
+  return TFE{ldexpf(m, -k), e + k};
+}
+
+__device__ __forceinline__ int fe_front32(const DeviceView& v, int r, int c, FeState& st) {
+  if (v.cardioid_mode == CARDIOID_PER_SAMPLE || !v.sa_min32) return kFront32Undecided;
+  const FFE er = v.eps32_re[c], ei = v.eps32_im[r];
+  const int ee = er.h == 0.0f ? ei.e : ei.h == 0.0f ? er.e : max(er.e, ei.e);
+  const CFF eps{ffe_scaled(er.h, er.l, er.e - ee), ffe_scaled(ei.h, ei.l, ei.e - ee), ee};
+  const int n = v.xlen;
+  int fire = n;
+  const float s = fmaf(eps.re.h, eps.re.h, eps.im.h * eps.im.h);  // |eps|^2 * 2^-2ee
+  if (s > 0.0f) {
+    const TFE u = tfe_norm(s, 2 * ee);
+    // both ends normalised (m in [1, 2)): the comparison is lexicographic
+    const TFE hi = tfe_norm(u.m * (1.0f + 0x1p-18f), u.e), lo = tfe_norm(u.m * (1.0f - 0x1p-18f), u.e);
+    const int i1 = first_below32(v.sa_min32, 1, n, hi);
+    if (i1 < n) {
+      if (first_below32(v.sa_min32, i1, n, lo) != i1) return kFront32Undecided;
+      fire = i1;
+    }
+  }
+  const int dsize = fire < n ? (fire - 3 < 1 ? 1 : fire - 3) : n;
+  const int found = dsize - 1;
+  // d[found] and its distance bound, both at exponent de
+  CFF d;
+  float dbound;  // in units of 2^d.e
+  if (found == 0) {
+    d = eps;
+    dbound = up_mul(0x1p-46f, cff_l1(eps));
+  } else {
+    const CFF e2 = cff_mul(eps, eps), e3 = cff_mul(eps, e2);
+    const CFF A = cff_of(v.sa_a32[found]), B = cff_of(v.sa_b32[found]), C = cff_of(v.sa_c32[found]);
+    const CFF ta = cff_mul(A, eps), tb = cff_mul(B, e2), tc = cff_mul(C, e3);
+    const float ma = cff_l1(ta), mb = cff_l1(tb), mc = cff_l1(tc);
+    int de = ma > 0.0f ? ta.e : -(1 << 29);
+    if (mb > 0.0f) de = max(de, tb.e);
+    if (mc > 0.0f) de = max(de, tc.e);
+    if (de == -(1 << 29)) de = ta.e;
+    d.e = de;
+    d.re = FF{0.0f, 0.0f};
+    d.im = FF{0.0f, 0.0f};
+    // products of the inputs' magnitudes bound each term's rounding
+    const float l1e = cff_l1(eps);
+    float mag = 0.0f;
+    const CFF* terms[3] = {&ta, &tb, &tc};
+    const float mags[3] = {up_mul(cff_l1(A), l1e), up_mul(up_mul(cff_l1(B), l1e), l1e),
+                           up_mul(up_mul(up_mul(cff_l1(C), l1e), l1e), l1e)};
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const int sh = terms[k]->e - de;
+      const float mk = up_add(mags[k], cff_l1(*terms[k]));
+      if (sh < -100) {  // below 2^-95 of the sum: dropped, its size in the bound
+        mag = up_add(mag, fmaxf(ldexpf(mk, sh + 40), 0x1p-126f));
+        continue;
+      }
+      d.re = ff_add(d.re, ff_scale(terms[k]->re, sh));
+      d.im = ff_add(d.im, ff_scale(terms[k]->im, sh));
+      mag = up_add(mag, fmaxf(ldexpf(mk, sh), 0x1p-126f));
+    }
+    dbound = up_mul(0x1p-40f, mag);
+  }
+  // escape before the stop is impossible when |X[found]| + |d| < 1023.5
+  {
+    const ZFF x = fe_load_z(v, found + 1);
+    const float dl1 = ldexpf(up_add(cff_l1(d), dbound), d.e);
+    const float xl1 = up_mul(up_add(fabsf(x.hx), fabsf(x.hy)), 1.0f + 0x1p-20f);
+    if (!(up_add(xl1, up_mul(dl1, 1.0f + 0x1p-20f)) < 1023.5f)) return kFront32Undecided;
+  }
+  // the state: delta and eps share exponent E below 2^-60, as fe_start does
+  const float dm = fmaxf(fabsf(d.re.h), fabsf(d.im.h));
+  const float em = fmaxf(fabsf(eps.re.h), fabsf(eps.im.h));
+  const int kNone = -(1 << 30);
+  const int mag = max(dm > 0.0f ? ilogbf(dm) + d.e : kNone, em > 0.0f ? ilogbf(em) + eps.e : kNone);
+  const int E = (mag > kNone && mag < kFeScaledBelow) ? mag : 0;
+  st.E = E;
+  st.dr = ffe_scaled(d.re.h, d.re.l, d.e - E);
+  st.di = ffe_scaled(d.im.h, d.im.l, d.e - E);
+  st.er = ffe_scaled(eps.re.h, eps.re.l, eps.e - E);
+  st.ei = ffe_scaled(eps.im.h, eps.im.l, eps.e - E);
+  st.err = up_add(fmaxf(ldexpf(dbound, d.e - E), 0.0f),
+                  up_mul(kFeU, up_add(fabsf(st.dr.h), fabsf(st.di.h))));
+  st.j = dsize;
+  st.i = dsize;
+  st.certified = 1;
+  st.frame = 0;
+  st.e64 = 0.0f;
+  st.pad_ = 0;
+  return kFront32Ready;
+}
+
+// The FE32 start state of sample (r, c): the FP32 front where it decides,
+// else the FP64 front.  True when the sample is finished in the front (out,
+// sm set); `fp64` tells which front ran.
+__device__ __forceinline__ bool fe_front_start(const DeviceView& v, int r, int c, FeState& st,
+                                               EscapeValue& out, double& sm, bool& undecided,
+                                               bool& fp64) {
+  undecided = false;
+  fp64 = false;
+  if (!v.double_loop && fe_front32(v, r, c, st) == kFront32Ready) return false;
+  fp64 = !v.double_loop;
+  SeriesFront f;
+  if (fe_front(v, r, c, f, out, sm, undecided)) return true;
+  fe_start(v, f, st);
+  return false;
+}
+
 // sqrt(x) from the hardware reciprocal square root (relative error below
 // 2^-21; 0 for x = 0).
 __device__ __forceinline__ float approx_sqrt(float x) {

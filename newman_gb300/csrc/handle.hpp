@@ -99,6 +99,13 @@ struct nm_handle {
   std::vector<nmg::RFE> eps_re_fe, eps_im_fe;
   DevBuf<nmg::RFE> d_eps_re_fe, d_eps_im_fe, d_sa_min_fe;
   DevBuf<nmg::CFE> d_a_fe, d_b_fe, d_c_fe;
+  // tables of the FP32 series front
+  std::vector<nmg::FFE> eps32_re, eps32_im;
+  std::vector<nmg::CFFE> a32, b32, c32;
+  std::vector<nmg::TFE> sa_min32;
+  DevBuf<nmg::FFE> d_eps32_re, d_eps32_im;
+  DevBuf<nmg::CFFE> d_a32, d_b32, d_c32;
+  DevBuf<nmg::TFE> d_sa_min32;
   int reference_mode = nmg::REFERENCE_PROBES;
 
   // scratch: work counters, statistics, and the FE32 rework list

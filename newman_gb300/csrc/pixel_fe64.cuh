@@ -120,7 +120,9 @@ NM_HD bool series_front_fe(const DeviceView& v, int r, int c, SeriesFront& f, Es
     return true;
   }
   const RFE er = v.eps_re_fe[c], ei = v.eps_im_fe[r];
-  const int e = er.e > ei.e ? er.e : ei.e;
+  // the shared exponent is the larger of the nonzero components' (a zero
+  // component -- the center row or column -- carries no exponent)
+  const int e = er.m == 0.0 ? ei.e : ei.m == 0.0 ? er.e : (er.e > ei.e ? er.e : ei.e);
   const CFE eps = cfe_norm({scalbn_(er.m, er.e - e), scalbn_(ei.m, ei.e - e), e});
   const CFE eps2 = cfe_sq(eps);
   const CFE eps3 = cfe_mul(eps, eps2);

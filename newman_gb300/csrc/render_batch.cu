@@ -66,16 +66,14 @@ __global__ void __launch_bounds__(256) batch_front_kernel(BatchGroup grp, FePass
       const DeviceView& v = grp.views[f];
       int r = 0, c = 0;
       if (sample_rc(v, g - grp.offsets[f], r, c)) {
-        SeriesFront fr;
         EscapeValue out;
         double sm = 0.0;
-        bool und = false;
-        if (fe_front(v, r, c, fr, out, sm, und)) {
+        bool und = false, fp64 = false;
+        FeState st;
+        if (fe_front_start(v, r, c, st, out, sm, und, fp64)) {
           store_sample(v, r, c, out, sm);
           finished++;
         } else {
-          FeState st;
-          fe_start(v, fr, st);
           st.frame = f;
           b.state[g] = st;
           needs_iteration = true;

@@ -36,10 +36,8 @@ struct FeJob {
   static constexpr int kCostWeight = 1;
   static __device__ __forceinline__ bool init(const DeviceView& v, int r, int c, State& st,
                                               EscapeValue& out, double& sm, bool& und) {
-    SeriesFront f;
-    if (fe_front(v, r, c, f, out, sm, und)) return true;
-    fe_start(v, f, st);
-    return false;
+    bool fp64;
+    return fe_front_start(v, r, c, st, out, sm, und, fp64);
   }
   static __device__ __forceinline__ bool steps(const DeviceView& v, State& st, int n,
                                                EscapeValue& out, double& sm,
@@ -69,7 +67,7 @@ __global__ void __launch_bounds__(256) fe_front_kernel(DeviceView v, FePassBuffe
                                                        unsigned long long* stats) {
   const unsigned kFull = 0xffffffffu;
   const int lane = threadIdx.x & 31;
-  unsigned long long finished = 0, undecided = 0;
+  unsigned long long finished = 0, undecided = 0, fp64_fronts = 0;
   const long long stride = (long long)gridDim.x * blockDim.x;
   // whole warps step together so that the list appends can be aggregated
   const long long span = ((total + 31) / 32) * 32;
@@ -78,18 +76,19 @@ __global__ void __launch_bounds__(256) fe_front_kernel(DeviceView v, FePassBuffe
     int r = 0, c = 0;
     bool needs_iteration = false;
     if (sid < total && sample_rc(v, sid, r, c)) {
-      SeriesFront f;
       EscapeValue out;
       double sm = 0.0;
-      bool und = false;
-      if (fe_front(v, r, c, f, out, sm, und)) {
+      bool und = false, fp64 = false;
+      FeState st;
+      if (fe_front_start(v, r, c, st, out, sm, und, fp64)) {
         store_sample(v, r, c, out, sm);
         finished++;
       } else {
-        fe_start(v, f, b.state[sid]);
+        b.state[sid] = st;
         needs_iteration = true;
       }
       undecided += und ? 1 : 0;
+      fp64_fronts += fp64 ? 1 : 0;
     }
     const unsigned want = __ballot_sync(kFull, needs_iteration);
     if (want) {
@@ -104,10 +103,12 @@ __global__ void __launch_bounds__(256) fe_front_kernel(DeviceView v, FePassBuffe
   for (int o = 16; o > 0; o >>= 1) {
     finished += __shfl_xor_sync(kFull, finished, o);
     undecided += __shfl_xor_sync(kFull, undecided, o);
+    fp64_fronts += __shfl_xor_sync(kFull, fp64_fronts, o);
   }
   if (lane == 0) {
     if (finished) atomicAdd(&stats[STAT_SAMPLES], finished);
     if (undecided) atomicAdd(&stats[STAT_CARDIOID_UNDECIDED], undecided);
+    if (fp64_fronts) atomicAdd(&stats[STAT_FRONT_FP64], fp64_fronts);
   }
 }
 

@@ -38,6 +38,22 @@ struct RFE {  // m * 2^e
   int32_t e;
 };
 
+// Tables of the FP32 series front (fe_front32.cuh), all normalised so that the
+// larger high word lies in [1, 2) (or is 0):
+struct alignas(16) FFE {   // (h + l) * 2^e: a real in float-float with an exponent
+  float h, l;
+  int32_t e, pad_;
+};
+struct alignas(16) CFFE {  // ((rh + rl) + i (ih + il)) * 2^e
+  float rh, rl, ih, il;
+  int32_t e, pad_[3];
+};
+struct TFE {               // m * 2^e, m in [1, 2); e = kTfeInf: +inf, kTfeZero: 0
+  float m;
+  int32_t e;
+};
+constexpr int32_t kTfeInf = 0x7fffffff, kTfeZero = -0x7fffffff;
+
 enum CardioidMode : int32_t {
   CARDIOID_PER_SAMPLE = 0,  // evaluate the test for each sample (double-double)
   CARDIOID_NONE = 1,        // the view box is provably outside both regions
@@ -81,6 +97,13 @@ struct DeviceView {
   const CFE* sa_b_fe;
   const CFE* sa_c_fe;
   const RFE* sa_min_fe;    // [xlen]
+  // the same for the FP32 series front (null: that front is not used)
+  const FFE* eps32_re;     // [nc]
+  const FFE* eps32_im;     // [nr]
+  const CFFE* sa_a32;      // [xlen]
+  const CFFE* sa_b32;
+  const CFFE* sa_c32;
+  const TFE* sa_min32;     // [xlen]
 
   EscapeValue* grid;       // [nr*nc]
   double* smooth64;        // optional [nr*nc] unrounded smoothing

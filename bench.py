@@ -461,6 +461,9 @@ def run_deep(args):
     nr, nc, N, bits = 2160, 3840, 1000000, 1100
     cre, cim, width = deep_view()
     getcontext().prec = 340
+    if args.profile:
+        # one FE32 render of a 1/DIV-size crop (same center and width): the ncu case
+        nr, nc = nr // args.profile, nc // args.profile
     step = str(Decimal(width) / nc)
 
     def make(path, rows=nr):
@@ -474,6 +477,12 @@ def run_deep(args):
     t0 = time.perf_counter()
     m.precompute()
     precompute_s = time.perf_counter() - t0
+    if args.profile:
+        m.render()
+        print("profile case %dx%d, FE32: %.1f ms, rework %d, FP64 fronts %d" % (
+            nr, nc, m.stat(nm.STAT_KERNEL_NS) * 1e-6, m.stat(nm.STAT_FP64_REWORK),
+            m.stat(nm.STAT_FRONT_FP64)))
+        return
     for _ in range(args.warmup):
         m.render()
     times = []

@@ -166,6 +166,26 @@ int nm_zoom_at(nm_handle* h, float scale, int r, int c, int sc);   /* mandelbrot
 int nm_load_legacy(nm_handle* h, const char* path);                /* mandelbrot.cpp:19-35 */
 int nm_save(const nm_handle* h, const char* path);                 /* viewer.cpp:12-23 */
 
+/* ---- colouring (multiwave.cpp, viewer.cpp:89-124) ---------------------------
+   nm_palette is MultiWaveGenerator: nm_palette_load reads its text format
+   (load_filename, multiwave.cpp:19-50; NULL on failure), nm_palette_save
+   writes it (save_filename, :52-73), nm_palette_cache is cache(n) (:75-116)
+   as n RGB triples.  nm_colorize is FractalViewer::colorLine over every row
+   (viewer.cpp:98-124) on the GPU: per pixel the palette colour of each of its
+   sc x sc samples (getColor, :89-94: black at N, the blend of the entries on
+   either side of the smoothed count when `smooth`), their float mean, into
+   rgb_out as (rows/sc) x (cols/sc) RGB bytes.  The reference takes HSL
+   conversion, blending and clipping from libbyteimage (not in the reference
+   tree); they are the standard definitions here (round half up). */
+typedef struct nm_palette nm_palette;
+nm_palette* nm_palette_load(const char* path);
+int nm_palette_save(const nm_palette* p, const char* path);
+void nm_palette_destroy(nm_palette* p);
+int nm_palette_cache(nm_palette* p, int n, unsigned char* rgb_out);
+int nm_colorize(nm_handle* h, nm_palette* p, int sc, int smooth, unsigned char* rgb_out);
+/* A binary PPM (P6) of rows x cols RGB bytes: headless image output. */
+int nm_write_ppm(const char* path, const unsigned char* rgb, int rows, int cols);
+
 /* ---- learned tile scheduling (no reference counterpart) ---------------------
    Tiles are the render's tiles of NM_OPT_TILE_W x NM_OPT_TILE_H samples,
    row-major ids over the whole grid.  nm_set_tile_order sets the order in

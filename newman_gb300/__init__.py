@@ -46,7 +46,8 @@ EXPORTS = (
     "nm_preview", "nm_tiles", "nm_set_tile_order", "nm_get_tile_costs", "nm_tile_features",
     "nm_cost_model_create", "nm_cost_model_destroy", "nm_cost_model_params",
     "nm_cost_model_set_params", "nm_cost_model_predict", "nm_cost_model_gradient",
-    "nm_cost_model_train",
+    "nm_cost_model_train", "nm_palette_load", "nm_palette_save", "nm_palette_destroy",
+    "nm_palette_cache", "nm_colorize", "nm_write_ppm",
 )
 
 
@@ -134,6 +135,12 @@ def load_library(path=LIB_PATH):
         "nm_cost_model_predict": (i32, [vp, vp, i32, vp]),
         "nm_cost_model_gradient": (i32, [vp, vp, vp, i32, vp, vp]),
         "nm_cost_model_train": (i32, [vp, vp, vp, i32, i32, ctypes.c_float, vp]),
+        "nm_palette_load": (vp, [cp]),
+        "nm_palette_save": (i32, [vp, cp]),
+        "nm_palette_destroy": (None, [vp]),
+        "nm_palette_cache": (i32, [vp, i32, vp]),
+        "nm_colorize": (i32, [vp, vp, i32, i32, vp]),
+        "nm_write_ppm": (i32, [cp, vp, i32, i32]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -200,6 +207,36 @@ class Batch:
         _check(_lib.nm_batch_autotune(self._b, int(stride), ctypes.byref(w), ctypes.byref(h),
                                       ctypes.byref(rn)))
         return w.value, h.value, rn.value
+
+
+class Palette:
+    """MultiWaveGenerator (multiwave.h:8-37) read from its text format."""
+
+    def __init__(self, path):
+        L = load_library()
+        self._p = L.nm_palette_load(_s(path))
+        if not self._p:
+            raise NewmanError(NM_ERR_IO, L.nm_last_error().decode())
+
+    def __del__(self):
+        p, self._p = getattr(self, "_p", None), None
+        if p and _lib is not None:
+            _lib.nm_palette_destroy(p)
+
+    def save(self, path):
+        _check(_lib.nm_palette_save(self._p, _s(path)))
+
+    def cache(self, n):
+        """cache(n) (multiwave.cpp:75-116) as an (n, 3) uint8 array."""
+        out = np.empty((n, 3), np.uint8)
+        _check(_lib.nm_palette_cache(self._p, int(n), out.ctypes.data))
+        return out
+
+
+def write_ppm(path, rgb):
+    """A binary PPM of an (rows, cols, 3) uint8 image."""
+    rgb = np.ascontiguousarray(rgb, dtype=np.uint8)
+    _check(load_library().nm_write_ppm(_s(path), rgb.ctypes.data, rgb.shape[0], rgb.shape[1]))
 
 
 class CostModel:
@@ -309,6 +346,14 @@ class Mandelbrot:
         out = np.empty(tx * ty, np.uint64)
         _check(_lib.nm_get_tile_costs(self._h, out.ctypes.data, out.size))
         return out.reshape(ty, tx)
+
+    def colorize(self, palette, sc=1, smooth=True):
+        """FractalViewer::colorLine over every row (viewer.cpp:98-124): the
+        image as (rows/sc, cols/sc, 3) uint8."""
+        out = np.empty((self.rows() // sc, self.cols() // sc, 3), np.uint8)
+        _check(_lib.nm_colorize(self._h, palette._p, int(sc), 1 if smooth else 0,
+                                out.ctypes.data))
+        return out
 
     def tile_features(self, tile_w, tile_h):
         """Features of this (rendered preview) grid's tiles of tile_w x tile_h

@@ -38,9 +38,12 @@ struct HwJob {
 // exponent (pixel_xd.cuh); the rest in plain doubles.  The choice is per view,
 // so a warp of one view never diverges on it.
 struct Delta64Job {
-  union State {
-    DeltaState d;
-    DeltaXDState x;
+  struct State {
+    union {
+      DeltaState d;
+      DeltaXDState x;
+    };
+    int32_t xd;  // 1: in the unbounded-exponent form
   };
   static constexpr bool kCertifies = false;
   static constexpr int kCostWeight = kCostFp64Step;
@@ -49,19 +52,36 @@ struct Delta64Job {
                                               EscapeValue& out, double& sm, bool& und) {
     SeriesFront f;
     if (series_front_any(v, r, c, f, out, sm, und)) return true;
-    if (v.sa_fe)
-      delta_xd_start(f, st.x);
-    else
+    st.xd = 0;
+    if (!v.sa_fe) {
       delta_start(f, st.d);
+    } else if (!delta_plain_start(f, st.d)) {
+      delta_xd_start(f, st.x);
+      st.xd = 1;
+    }
     return false;
   }
   static __device__ __forceinline__ bool steps(const DeviceView& v, State& st, int n,
                                                EscapeValue& out, double& sm,
                                                unsigned long long& executed,
                                                unsigned long long&) {
-    const int before = v.sa_fe ? st.x.i : st.d.i;
-    const bool done = v.sa_fe ? delta_xd_steps(v, st.x, n, out, sm) : delta_steps(v, st.d, n, out, sm);
-    const int after = v.sa_fe ? st.x.i : st.d.i;
+    const int before = st.xd ? st.x.i : st.d.i;
+    bool done;
+    if (!v.sa_fe) {
+      done = delta_steps(v, st.d, n, out, sm);
+    } else if (st.xd) {
+      done = delta_xd_steps(v, st.x, n, out, sm);
+    } else {
+      bool handover;
+      done = delta_guarded_steps(v, st.d, n, out, sm, handover);
+      if (handover) {  // the rest of the chunk in the unbounded-exponent form
+        const int left = n - (st.d.i - before);
+        delta_to_xd(st.d, st.x);
+        st.xd = 1;
+        done = left > 0 ? delta_xd_steps(v, st.x, left, out, sm) : false;
+      }
+    }
+    const int after = st.xd ? st.x.i : st.d.i;
     executed += (unsigned long long)((done ? out.iterations + (out.iterations < v.N ? 1 : 0)
                                            : after) - before);
     return done;

@@ -73,4 +73,109 @@ NM_HD bool delta_xd_steps(const DeviceView& v, DeltaXDState& st, int steps, Esca
   return false;
 }
 
+// ---- plain doubles while nothing comes near the underflow range ------------
+//
+// On a floatexp view most samples never bring a value of the delta step near
+// 2^-1022: then the plain double operations round exactly as the unbounded-
+// exponent ones (a double operation rounds like unbounded arithmetic whenever
+// its result is normal).  delta_guarded_steps runs the plain step and checks
+// its operands and results; a step that has a nonzero value below 2^-400
+// (where a product could underflow) is not taken -- the state before it,
+// exact in both forms, moves to DeltaXDState and the step runs there.
+
+// Nonzero and below 2^-400 (biased exponent field under 623).
+NM_HD bool near_underflow(double x) {
+  const int64_t b = xd_bits_(x);
+  return ((b >> 52) & 0x7ff) < 623 && (b & 0x7fffffffffffffffll) != 0;
+}
+
+// eps and d[found] of an FE front as plain doubles, when each is exactly
+// representable with room to spare (zero, or a normal double of at least
+// 2^-400 for delta; zero or normal for eps, which is only ever added).
+NM_HD bool delta_plain_start(const SeriesFront& f, DeltaState& st) {
+  const double dr = scalbn_d(f.dfound.re, f.d_e), di = scalbn_d(f.dfound.im, f.d_e);
+  const double er = scalbn_d(f.eps.re, f.eps_e), ei = scalbn_d(f.eps.im, f.eps_e);
+  auto normal_or_zero = [](double x) {
+    const int e = exp_field(x);
+    return x == 0.0 || (e >= 1 && e <= 2045);
+  };
+  if (near_underflow(dr) || near_underflow(di) || !normal_or_zero(dr) || !normal_or_zero(di) ||
+      !normal_or_zero(er) || !normal_or_zero(ei))
+    return false;
+  // the scalbn results are exact here: the FE mantissas carry 53 bits
+  if (scalbn_d(dr, -f.d_e) != f.dfound.re || scalbn_d(di, -f.d_e) != f.dfound.im ||
+      scalbn_d(er, -f.eps_e) != f.eps.re || scalbn_d(ei, -f.eps_e) != f.eps.im)
+    return false;
+  st.dr = dr;
+  st.di = di;
+  st.er = er;
+  st.ei = ei;
+  st.j = f.dsize;
+  st.i = f.dsize;
+  return true;
+}
+
+// delta_steps with the guard; `handover` is set when a step was left to the
+// unbounded-exponent form (st is the exact state before it).
+NM_HD bool delta_guarded_steps(const DeviceView& v, DeltaState& st, int steps, EscapeValue& out,
+                               double& sm, bool& handover) {
+  double dr = st.dr, di = st.di;
+  int j = st.j, i = st.i;
+  const int zlast = v.zlen - 1;
+  const int stop = (v.N - i < steps) ? v.N : i + steps;
+  handover = false;
+  for (; i < stop; i++) {
+    const Dbl2 z = v.z[j];
+    const double tr = add_(twice_(z.x), dr);
+    const double ti = add_(twice_(z.y), di);
+    const double nre = add_(sub_(mul_(tr, dr), mul_(ti, di)), st.er);
+    const double nim = add_(add_(mul_(tr, di), mul_(ti, dr)), st.ei);
+    const Dbl2 zn = v.z[j + 1];
+    const double yr = add_(zn.x, nre), yi = add_(zn.y, nim);
+    if (near_underflow(tr) || near_underflow(ti) || near_underflow(nre) || near_underflow(nim) ||
+        near_underflow(yr) || near_underflow(yi)) {
+      handover = true;  // state (dr, di, j, i) is before this step
+      break;
+    }
+    dr = nre;
+    di = nim;
+    j++;
+    const double r2 = add_(mul_(yr, yr), mul_(yi, yi));
+    if (above_bits(r2, v.bailout2)) {
+      sm = smoothing_of(r2, v.log_bailout);
+      out = {i, (float)sm};
+      return true;
+    }
+    bool rebase = j == zlast;
+    if (!rebase && !clearly_larger(yr, yi, dr, di))
+      rebase = above_bits(add_(mul_(dr, dr), mul_(di, di)), r2);
+    if (rebase) {
+      dr = yr;
+      di = yi;
+      j = 0;
+    }
+  }
+  st.dr = dr;
+  st.di = di;
+  st.j = j;
+  st.i = i;
+  if (handover) return false;
+  if (i >= v.N) {
+    out = {v.N, 0.0f};
+    sm = 0.0;
+    return true;
+  }
+  return false;
+}
+
+NM_HD void delta_to_xd(const DeltaState& d, DeltaXDState& x) {
+  const DeltaState c = d;  // d and x may share storage
+  x.dr = xd_of(c.dr);
+  x.di = xd_of(c.di);
+  x.er = xd_of(c.er);
+  x.ei = xd_of(c.ei);
+  x.j = c.j;
+  x.i = c.i;
+}
+
 }  // namespace nmg

@@ -994,6 +994,139 @@ int nmo_reduce(int nr, int nc, int sc, const int32_t* iters, const float* smooth
   return 0;
 }
 
+// ---- colouring: multiwave.cpp:5-116 and viewer.cpp:89-124 --------------------
+// libbyteimage's helpers (absent from the reference tree) as their standard
+// definitions: clip rounds half up into [0, 255]; interp blends per channel;
+// hsl2rgb is the usual six-sector map.
+namespace colour {
+unsigned char clip(float x) {
+  if (x > 0.0f) return x >= 255.0f ? 255 : (unsigned char)(x + 0.5f);
+  return 0;
+}
+struct C3 {
+  unsigned char c[3];
+};
+C3 blend(C3 a, C3 b, float t) {
+  C3 o;
+  for (int k = 0; k < 3; k++) o.c[k] = clip((1.0f - t) * a.c[k] + t * b.c[k]);
+  return o;
+}
+C3 hsl(float h, float s, float l) {
+  float hue = std::fmod(h, 360.0f);
+  if (hue < 0.0f) hue += 360.0f;
+  const float chroma = (1.0f - std::fabs(2.0f * l - 1.0f)) * s;
+  const float sector = hue / 60.0f;
+  const float mid = chroma * (1.0f - std::fabs(std::fmod(sector, 2.0f) - 1.0f));
+  const float tab[6][3] = {{chroma, mid, 0.0f}, {mid, chroma, 0.0f}, {0.0f, chroma, mid},
+                           {0.0f, mid, chroma}, {mid, 0.0f, chroma}, {chroma, 0.0f, mid}};
+  const float* t = tab[(int)sector % 6];
+  const float base = l - 0.5f * chroma;
+  C3 o;
+  for (int k = 0; k < 3; k++) o.c[k] = clip(255.0f * (t[k] + base));
+  return o;
+}
+struct Cycle {
+  std::vector<float> v;
+  int period = 1;
+  // (1.0 - t) promotes the blend to double (multiwave.cpp:11)
+  float at(int step) const {
+    float t = (int)v.size() * (step % period) / (float)period;
+    int i0 = (int)t;
+    t -= i0;
+    return (float)((1.0 - t) * v[i0] + t * v[(i0 + 1) % v.size()]);
+  }
+};
+struct Palette {
+  std::vector<Cycle> hue;
+  int hue_period = 1;
+  Cycle sat;
+  std::vector<std::pair<float, int>> waves;  // amplitude, period
+};
+bool read_palette(const char* path, Palette& p) {
+  std::FILE* fp = std::fopen(path, "r");
+  if (!fp) return false;
+  auto cycle = [&](Cycle& c) {
+    int n = 0;
+    if (std::fscanf(fp, "%d", &n) != 1 || n < 1) return false;
+    c.v.assign(n, 0.0f);
+    for (float& x : c.v)
+      if (std::fscanf(fp, "%f", &x) != 1) return false;
+    return std::fscanf(fp, "%d", &c.period) == 1 && c.period > 0;
+  };
+  int n = 0;
+  bool ok = std::fscanf(fp, "%d", &n) == 1 && n > 0;
+  if (ok) p.hue.resize(n);
+  for (Cycle& c : p.hue) ok = ok && cycle(c);
+  ok = ok && std::fscanf(fp, "%d", &p.hue_period) == 1 && p.hue_period > 0;
+  ok = ok && cycle(p.sat);
+  ok = ok && std::fscanf(fp, "%d", &n) == 1 && n >= 0;
+  if (ok) p.waves.resize(n);
+  for (auto& w : p.waves) ok = ok && std::fscanf(fp, "%f %d", &w.first, &w.second) == 2 && w.second > 0;
+  std::fclose(fp);
+  return ok;
+}
+std::vector<C3> cache(const Palette& p, int n) {
+  constexpr float tau = 2.0 * 3.14159265358979;  // multiwave.cpp:15
+  std::vector<C3> out(n);
+  for (int i = 0; i < n; i++) {
+    const float sat = p.sat.at(i);
+    float lum = 0.0f;
+    for (auto& w : p.waves) lum += w.first * std::sin(i * tau / w.second);
+    lum = 1.0 / (1.0 + std::exp(-lum));
+    auto along = [&](const Cycle& c) {
+      float tx = (int)c.v.size() * (i % c.period) / (float)c.period;
+      int x0 = (int)tx;
+      tx -= x0;
+      return blend(hsl(c.v[x0], sat, lum), hsl(c.v[(x0 + 1) % c.v.size()], sat, lum), tx);
+    };
+    float ty = (int)p.hue.size() * (i % p.hue_period) / (float)p.hue_period;
+    int y0 = (int)ty;
+    ty -= y0;
+    out[i] = blend(along(p.hue[y0]), along(p.hue[(y0 + 1) % p.hue.size()]), ty);
+  }
+  return out;
+}
+}  // namespace colour
+
+int nmo_palette_cache(const char* path, int n, unsigned char* out) {
+  colour::Palette p;
+  if (!colour::read_palette(path, p)) return 1;
+  auto pal = colour::cache(p, n);
+  for (int i = 0; i < n; i++)
+    for (int k = 0; k < 3; k++) out[3 * i + k] = pal[i].c[k];
+  return 0;
+}
+
+// getColor + colorLine (viewer.cpp:89-124) over a sample grid; pal is the
+// cached palette as RGB triples (npal >= N).
+int nmo_colorize(const int32_t* iters, const float* smooth, int nr, int nc, int N,
+                 const unsigned char* pal, int sc, int smooth_flag, unsigned char* out) {
+  auto entry = [&](int k) {
+    colour::C3 c;
+    for (int q = 0; q < 3; q++) c.c[q] = pal[3 * k + q];
+    return c;
+  };
+  for (int r = 0; r < nr / sc; r++)
+    for (int c = 0; c < nc / sc; c++) {
+      float acc[3] = {0.0f, 0.0f, 0.0f};
+      for (int r1 = r * sc; r1 < (r + 1) * sc; r1++)
+        for (int c1 = c * sc; c1 < (c + 1) * sc; c1++) {
+          const long k = (long)r1 * nc + c1;
+          colour::C3 col = {{0, 0, 0}};
+          if (iters[k] < N) {
+            col = smooth_flag ? colour::blend(entry(iters[k] > 0 ? iters[k] - 1 : 0),
+                                              entry(iters[k]), smooth[k])
+                              : entry(iters[k]);
+          }
+          for (int q = 0; q < 3; q++) acc[q] += col.c[q];
+        }
+      unsigned char* o = out + 3 * ((long)r * (nc / sc) + c);
+      for (int q = 0; q < 3; q++)
+        o[q] = sc == 1 ? (unsigned char)acc[q] : colour::clip(acc[q] / (float)(sc * sc));
+    }
+  return 0;
+}
+
 // Decimal string of the center / step (for carrying views between handles).
 int nmo_get_view(nmo_view* h, int which, char* buf, int buflen) {
   View* v = reinterpret_cast<View*>(h);

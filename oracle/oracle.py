@@ -48,6 +48,8 @@ def lib():
         L.nmo_series_skip.argtypes = [vp, ctypes.c_long, P(ctypes.c_int32), P(ctypes.c_int32),
                                       P(ctypes.c_int32)]
         L.nmo_get_view.argtypes = [vp, i32, ctypes.c_char_p, i32]
+        L.nmo_palette_cache.argtypes = [ctypes.c_char_p, i32, vp]
+        L.nmo_colorize.argtypes = [vp, vp, i32, i32, i32, vp, i32, i32, vp]
         _lib = L
     return _lib
 
@@ -170,3 +172,23 @@ def reduce(iters, smooth, sc):
     lib().nmo_reduce(nr, nc, sc, _p(iters, ctypes.c_int32), _p(smooth, ctypes.c_float),
                      _p(oi, ctypes.c_int32), _p(os_, ctypes.c_float))
     return oi, os_
+
+
+def palette_cache(path, n):
+    """MultiWaveGenerator::cache(n) of the palette file at `path`: (n, 3) uint8."""
+    out = np.empty((n, 3), np.uint8)
+    if lib().nmo_palette_cache(str(path).encode(), int(n), out.ctypes.data):
+        raise IOError("cannot read palette %s" % path)
+    return out
+
+
+def colorize(iters, smooth, N, pal, sc, smooth_flag=True):
+    """colorLine over every row: (rows/sc, cols/sc, 3) uint8."""
+    iters = np.ascontiguousarray(iters, dtype=np.int32)
+    smooth = np.ascontiguousarray(smooth, dtype=np.float32)
+    pal = np.ascontiguousarray(pal, dtype=np.uint8)
+    nr, nc = iters.shape
+    out = np.empty((nr // sc, nc // sc, 3), np.uint8)
+    lib().nmo_colorize(iters.ctypes.data, smooth.ctypes.data, nr, nc, int(N), pal.ctypes.data,
+                       int(sc), 1 if smooth_flag else 0, out.ctypes.data)
+    return out

@@ -183,6 +183,15 @@ int nm_palette_save(const nm_palette* p, const char* path);
 void nm_palette_destroy(nm_palette* p);
 int nm_palette_cache(nm_palette* p, int n, unsigned char* rgb_out);
 int nm_colorize(nm_handle* h, nm_palette* p, int sc, int smooth, unsigned char* rgb_out);
+/* VideoZoom::nextFrame (video.cpp:14-34) on the GPU: the `rate` frames between
+   keyframes prev and cur (key_rows x key_cols RGB, rendered at 1.5 times the
+   frame size as the viewer's auto-zoom does, viewer.cpp:270-286), as
+   rate x rows x cols RGB bytes in frames_out.  The reference writes them to
+   an AVI; here they are returned (headless).  libbyteimage's scaled / blend
+   are restated as bilinear resampling and a per-channel blend. */
+int nm_video_interpolate(const unsigned char* prev_rgb, const unsigned char* cur_rgb,
+                         int key_rows, int key_cols, int rows, int cols, int rate,
+                         unsigned char* frames_out);
 /* A binary PPM (P6) of rows x cols RGB bytes: headless image output. */
 int nm_write_ppm(const char* path, const unsigned char* rgb, int rows, int cols);
 

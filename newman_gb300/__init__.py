@@ -47,7 +47,7 @@ EXPORTS = (
     "nm_cost_model_create", "nm_cost_model_destroy", "nm_cost_model_params",
     "nm_cost_model_set_params", "nm_cost_model_predict", "nm_cost_model_gradient",
     "nm_cost_model_train", "nm_palette_load", "nm_palette_save", "nm_palette_destroy",
-    "nm_palette_cache", "nm_colorize", "nm_write_ppm",
+    "nm_palette_cache", "nm_colorize", "nm_write_ppm", "nm_video_interpolate",
 )
 
 
@@ -141,6 +141,7 @@ def load_library(path=LIB_PATH):
         "nm_palette_cache": (i32, [vp, i32, vp]),
         "nm_colorize": (i32, [vp, vp, i32, i32, vp]),
         "nm_write_ppm": (i32, [cp, vp, i32, i32]),
+        "nm_video_interpolate": (i32, [vp, vp, i32, i32, i32, i32, i32, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -237,6 +238,21 @@ def write_ppm(path, rgb):
     """A binary PPM of an (rows, cols, 3) uint8 image."""
     rgb = np.ascontiguousarray(rgb, dtype=np.uint8)
     _check(load_library().nm_write_ppm(_s(path), rgb.ctypes.data, rgb.shape[0], rgb.shape[1]))
+
+
+def video_interpolate(prev, cur, rows, cols, rate):
+    """VideoZoom::nextFrame (video.cpp:14-34): the `rate` frames between two
+    keyframes ((kh, kw, 3) uint8, kh >= rows, kw >= cols) as
+    (rate, rows, cols, 3) uint8."""
+    prev = np.ascontiguousarray(prev, dtype=np.uint8)
+    cur = np.ascontiguousarray(cur, dtype=np.uint8)
+    if prev.shape != cur.shape or prev.ndim != 3 or prev.shape[2] != 3:
+        raise ValueError("keyframes must be two (rows, cols, 3) images of one size")
+    out = np.empty((rate, rows, cols, 3), np.uint8)
+    _check(load_library().nm_video_interpolate(prev.ctypes.data, cur.ctypes.data, prev.shape[0],
+                                               prev.shape[1], int(rows), int(cols), int(rate),
+                                               out.ctypes.data))
+    return out
 
 
 class CostModel:

@@ -1127,6 +1127,55 @@ int nmo_colorize(const int32_t* iters, const float* smooth, int nr, int nc, int 
   return 0;
 }
 
+// VideoZoom::nextFrame (video.cpp:14-34): `rate` frames between two keyframes.
+// ByteImage::scaled restated as bilinear resampling (pixel centres aligned),
+// blend as (1 - t) a + t b, both rounded half up (libbyteimage is absent).
+int nmo_video_interpolate(const unsigned char* prev, const unsigned char* cur, int kh, int kw,
+                          int nr, int nc, int rate, unsigned char* out) {
+  auto scaled = [](const unsigned char* src, int sh, int sw, int dh, int dw) {
+    std::vector<unsigned char> dst((size_t)dh * dw * 3);
+    const float ry = (float)sh / (float)dh, rx = (float)sw / (float)dw;
+    for (int y = 0; y < dh; y++)
+      for (int x = 0; x < dw; x++) {
+        float fy = ((float)y + 0.5f) * ry - 0.5f, fx = ((float)x + 0.5f) * rx - 0.5f;
+        fy = std::min(std::max(fy, 0.0f), (float)(sh - 1));
+        fx = std::min(std::max(fx, 0.0f), (float)(sw - 1));
+        const int y0 = (int)fy, x0 = (int)fx;
+        const int y1 = std::min(y0 + 1, sh - 1), x1 = std::min(x0 + 1, sw - 1);
+        const float wy = fy - (float)y0, wx = fx - (float)x0;
+        for (int k = 0; k < 3; k++) {
+          const float a = src[((long)y0 * sw + x0) * 3 + k], b = src[((long)y0 * sw + x1) * 3 + k];
+          const float c = src[((long)y1 * sw + x0) * 3 + k], d = src[((long)y1 * sw + x1) * 3 + k];
+          const float top = (1.0f - wx) * a + wx * b, bot = (1.0f - wx) * c + wx * d;
+          dst[((size_t)y * dw + x) * 3 + k] = colour::clip((1.0f - wy) * top + wy * bot);
+        }
+      }
+    return dst;
+  };
+  std::vector<unsigned char> canvas((size_t)nr * nc * 3, 0);
+  float v = std::pow(1.5, 1.0 / rate), sm = 2.0 / 3.0, lg = 1.0;
+  for (int i = 0; i < rate; i++) {
+    const float t = (float)i / rate;
+    const int sh = (int)(kh * sm), sw = (int)(kw * sm), lh = (int)(kh * lg), lw = (int)(kw * lg);
+    const auto small = scaled(cur, kh, kw, sh, sw);
+    const auto large = scaled(prev, kh, kw, lh, lw);
+    const int lr = (nr - lh) / 2, lc = (nc - lw) / 2, sr = (nr - sh) / 2, sc = (nc - sw) / 2;
+    for (int r = 0; r < nr; r++)
+      for (int c = 0; c < nc; c++) {
+        unsigned char* px = &canvas[((size_t)r * nc + c) * 3];
+        if (r - lr >= 0 && r - lr < lh && c - lc >= 0 && c - lc < lw)
+          for (int k = 0; k < 3; k++) px[k] = large[((size_t)(r - lr) * lw + (c - lc)) * 3 + k];
+        if (r - sr >= 0 && r - sr < sh && c - sc >= 0 && c - sc < sw)
+          for (int k = 0; k < 3; k++)
+            px[k] = colour::clip((1.0f - t) * px[k] + t * small[((size_t)(r - sr) * sw + (c - sc)) * 3 + k]);
+      }
+    std::memcpy(out + (size_t)i * nr * nc * 3, canvas.data(), canvas.size());
+    sm *= v;
+    lg *= v;
+  }
+  return 0;
+}
+
 // Decimal string of the center / step (for carrying views between handles).
 int nmo_get_view(nmo_view* h, int which, char* buf, int buflen) {
   View* v = reinterpret_cast<View*>(h);

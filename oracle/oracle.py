@@ -50,6 +50,7 @@ def lib():
         L.nmo_get_view.argtypes = [vp, i32, ctypes.c_char_p, i32]
         L.nmo_palette_cache.argtypes = [ctypes.c_char_p, i32, vp]
         L.nmo_colorize.argtypes = [vp, vp, i32, i32, i32, vp, i32, i32, vp]
+        L.nmo_video_interpolate.argtypes = [vp, vp, i32, i32, i32, i32, i32, vp]
         _lib = L
     return _lib
 
@@ -191,4 +192,15 @@ def colorize(iters, smooth, N, pal, sc, smooth_flag=True):
     out = np.empty((nr // sc, nc // sc, 3), np.uint8)
     lib().nmo_colorize(iters.ctypes.data, smooth.ctypes.data, nr, nc, int(N), pal.ctypes.data,
                        int(sc), 1 if smooth_flag else 0, out.ctypes.data)
+    return out
+
+
+def video_interpolate(prev, cur, rows, cols, rate):
+    """VideoZoom::nextFrame's `rate` frames between keyframes prev and cur
+    ((kh, kw, 3) uint8 each): (rate, rows, cols, 3) uint8."""
+    prev = np.ascontiguousarray(prev, dtype=np.uint8)
+    cur = np.ascontiguousarray(cur, dtype=np.uint8)
+    out = np.empty((rate, rows, cols, 3), np.uint8)
+    lib().nmo_video_interpolate(prev.ctypes.data, cur.ctypes.data, prev.shape[0], prev.shape[1],
+                                rows, cols, rate, out.ctypes.data)
     return out

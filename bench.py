@@ -523,6 +523,7 @@ def run_deep(args):
                    "reference": "orbit at the view center, floatexp series"},
         "orbit_length": m.stat(nm.STAT_ORBIT_LENGTH), "precompute_s": precompute_s,
         "executed_iters_per_step": executed, "effective_iters_per_step": eff,
+        "step_ms": [round(t, 3) for t in times],
         "fp64_rework_samples": rework, "fp64_front_samples": front_fp64, "max_escape": int(g[g < N].max()) if (g < N).any() else None,
         "interior_fraction": float((g == N).mean()),
         "fp64_band": {"rows": [r0, r0 + band], "ms": fp_ms, "value": fp_rate,

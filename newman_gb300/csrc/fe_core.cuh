@@ -40,6 +40,18 @@ namespace nmg {
 constexpr int kFeScaledBelow = -60;   // delta kept as mantissa * 2^E below 2^-60
 constexpr float kFeU = 0x1.2p-43f;    // float-float multiply-add rounding per step (worst case)
 constexpr float kFeUZ = 0x1p-45f;     // Z's representation and the rounding of t = 2Z + delta
+// u (1 + 2^-22) + u_z, rounded up: the two local terms on one product.  The
+// float-float t = 2Z + delta has |t.h|_1 <= (2|Z.h|_1 + |delta.h|_1)(1 + 2^-22.9)
+// (both inputs' low words are within 2^-24 of their high words, and t.h is
+// their sum rounded once more), so
+//   u |t.h|_1 |delta| + u_z (2|Z| + |delta|) |delta| <= kFeUT (2|Z| + |delta|) |delta|.
+constexpr float kFeUT = 0x1.61p-43f;
+// A bound below which the bailout test of a state with |Y|^2 <= 2^20 (1 - 2^-10)
+// and Z not the orbit's escaped last point is decided without evaluating it:
+// |Z.h|_1 < 1449, |delta.h|_1 < 2900, so the band of the full test,
+// 2 (2^-20 (|Z| + |delta|) + e + u_z |Z| + u (|Z| + |delta|)), stays below
+// 2 (0.0043 + e + 2^-30) < 0.49 <= 1024 - |Y| whenever e < 0.2.
+constexpr float kFeQuickErr = 0.2f;
 constexpr float kFeBailout = 1024.0f;       // mandelbrot.cpp:58
 constexpr float kFeBailout2 = 1048576.0f;   // mandelbrot.cpp:59
 
@@ -376,9 +388,8 @@ __device__ __forceinline__ bool fe_scaled_steps(const DeviceView& v, FeState& st
       const float dmag = fmaxf(ldexpf(dl1, st.E), 0x1p-126f);
       const float amp = up_add(up_mul(2.0f, up_add(zl1, dmag)),
                                fmaxf(ldexpf(st.err, st.E), 0x1p-126f));
-      const float loc = up_fma(kFeU, up_fma(up_add(fabsf(tr.h), fabsf(ti.h)), dl1,
-                                            up_add(fabsf(st.er.h), fabsf(st.ei.h))),
-                               up_mul(kFeUZ, up_mul(up_fma(2.0f, zl1, dmag), dl1)));
+      const float loc = up_fma(kFeUT, up_mul(up_fma(2.0f, zl1, dmag), dl1),
+                               up_mul(kFeU, up_add(fabsf(st.er.h), fabsf(st.ei.h))));
       st.err = up_fma(amp, st.err, loc);
     }
     st.dr = nr;
@@ -458,7 +469,7 @@ __device__ __forceinline__ bool fe_advance(const DeviceView& v, FeState& st, int
   const int stop = min(v.N, st.i + steps);
   const int start = st.i;
   const float lo_band = kFeBailout2 * (1.0f - 0x1p-10f);
-  const float eps_l1 = up_add(fabsf(st.er.h), fabsf(st.ei.h));
+  const float ueps = up_mul(kFeU, up_add(fabsf(st.er.h), fabsf(st.ei.h)));
   const FF er = st.er, ei = st.ei;
   FF dr = st.dr, di = st.di;
   float err = st.err;
@@ -478,8 +489,7 @@ __device__ __forceinline__ bool fe_advance(const DeviceView& v, FeState& st, int
     const FF ti = ff_add(FF{2.0f * z.hy, 2.0f * z.ly}, di);
     const float zl1 = up_add(fabsf(z.hx), fabsf(z.hy)), dl1 = up_add(fabsf(dr.h), fabsf(di.h));
     const float ym_up = up_fma(0x1p-20f, up_add(zl1, dl1), ym);
-    const float loc = up_fma(kFeU, up_fma(up_add(fabsf(tr.h), fabsf(ti.h)), dl1, eps_l1),
-                             up_mul(kFeUZ, up_mul(up_fma(2.0f, zl1, dl1), dl1)));
+    const float loc = up_fma(kFeUT, up_mul(up_fma(2.0f, zl1, dl1), dl1), ueps);
     const float err_old = err;
     err = up_fma(up_fma(2.0f, ym_up, err), err, loc);  // 2|Y| e + e^2 + local rounding
     FF nr, ni;
@@ -491,50 +501,60 @@ __device__ __forceinline__ bool fe_advance(const DeviceView& v, FeState& st, int
     const float yr = z.hx + dr.h, yi = z.hy + di.h;
     const float r2 = fmaf(yr, yr, yi * yi);
     ym = approx_sqrt(r2);
-    const float zn1 = up_add(fabsf(z.hx), fabsf(z.hy)), dn1 = up_add(fabsf(dr.h), fabsf(di.h));
     // error of Y = Z + delta held in float-float (the rebase value)
-    const float yerr_fe = up_add(err, up_fma(kFeUZ, zn1, up_mul(kFeU, up_add(zn1, dn1))));
-    float yerr = yerr_fe;
-    if (dloop) {
-      // The double loop's own distance from exact arithmetic, d' <= (|z| + |w|) d
-      // + its rounding: with |w| <= |Y| + e (the exact orbit) and |z| <= |w| + d,
-      // d' <= (2(|Y| + e) + d) d + 2^-52 (2 |z|^2 + |z'|_1); its bailout test
-      // rounds |z|^2 by 2^-52 more.  The tests below take the sum of both bounds.
-      const float w_old = up_add(ym_up, err_old);
-      const float z_old = up_add(w_old, e64);
-      const float z_new = up_add(up_add(zn1, dn1), up_add(err, e64));
-      const float l64 = up_mul(0x1p-52f, up_fma(up_mul(2.0f, z_old), z_old, z_new));
-      e64 = up_fma(up_fma(2.0f, w_old, e64), e64, l64);
-      yerr = up_add(yerr, up_fma(0x1p-52f, z_new, e64));
-    }
-    if (r2 <= lo_band) {
-      // |Y| is below the bailout by more than 2^-11 of it; the estimate ym
-      // is good to 2^-20 (|Z| + |delta|), so the test is decided unless the
-      // bound covers the whole gap
-      if (up_mul(2.0f, up_fma(0x1p-20f, up_add(zn1, dn1), yerr)) >= __fsub_rd(kFeBailout, ym)) {
-        certified = false;  // the FP64 kernel renders this sample
-        done = true;
-        i++;
-        break;
+    auto y_err = [&]() {
+      const float zn1 = up_add(fabsf(z.hx), fabsf(z.hy)), dn1 = up_add(fabsf(dr.h), fabsf(di.h));
+      return up_add(err, up_fma(kFeUZ, zn1, up_mul(kFeU, up_add(zn1, dn1))));
+    };
+    // The bailout test: evaluated in full near the bailout, on a double-loop
+    // view (whose second bound e64 is propagated every step), at the orbit's
+    // last point, or once the bound has grown past kFeQuickErr; otherwise it
+    // is decided (|Y| below 1024 by more than the band) -- see kFeQuickErr.
+    if (dloop || r2 > lo_band || !(err < kFeQuickErr) || j == zlast) {
+      const float zn1 = up_add(fabsf(z.hx), fabsf(z.hy)), dn1 = up_add(fabsf(dr.h), fabsf(di.h));
+      float yerr = y_err();
+      if (dloop) {
+        // The double loop's own distance from exact arithmetic, d' <= (|z| + |w|) d
+        // + its rounding: with |w| <= |Y| + e (the exact orbit) and |z| <= |w| + d,
+        // d' <= (2(|Y| + e) + d) d + 2^-52 (2 |z|^2 + |z'|_1); its bailout test
+        // rounds |z|^2 by 2^-52 more.  The tests below take the sum of both bounds.
+        const float w_old = up_add(ym_up, err_old);
+        const float z_old = up_add(w_old, e64);
+        const float z_new = up_add(up_add(zn1, dn1), up_add(err, e64));
+        const float l64 = up_mul(0x1p-52f, up_fma(up_mul(2.0f, z_old), z_old, z_new));
+        e64 = up_fma(up_fma(2.0f, w_old, e64), e64, l64);
+        yerr = up_add(yerr, up_fma(0x1p-52f, z_new, e64));
       }
-    } else {
-      FF r2ff;
-      if (fe_escape_test(ff_add(FF{z.hx, z.lx}, dr), ff_add(FF{z.hy, z.ly}, di), yerr,
-                         certified, r2ff)) {
-        res.it = i;
-        res.r2 = r2ff;
-        done = true;
-        i++;
-        break;
-      }
-      if (!certified) {
-        done = true;
-        i++;
-        break;
+      if (r2 <= lo_band) {
+        // |Y| is below the bailout by more than 2^-11 of it; the estimate ym
+        // is good to 2^-20 (|Z| + |delta|), so the test is decided unless the
+        // bound covers the whole gap
+        if (up_mul(2.0f, up_fma(0x1p-20f, up_add(zn1, dn1), yerr)) >= __fsub_rd(kFeBailout, ym)) {
+          certified = false;  // the FP64 kernel renders this sample
+          done = true;
+          i++;
+          break;
+        }
+      } else {
+        FF r2ff;
+        if (fe_escape_test(ff_add(FF{z.hx, z.lx}, dr), ff_add(FF{z.hy, z.ly}, di), yerr,
+                           certified, r2ff)) {
+          res.it = i;
+          res.r2 = r2ff;
+          done = true;
+          i++;
+          break;
+        }
+        if (!certified) {
+          done = true;
+          i++;
+          break;
+        }
       }
     }
     const float d2 = fmaf(dr.h, dr.h, di.h * di.h);
     if (r2 < d2 || j == zlast) {  // rebase to Z[0]: delta = Y in float-float
+      const float yerr_fe = y_err();
       const FF nyr = ff_add(FF{z.hx, z.lx}, dr);
       const FF nyi = ff_add(FF{z.hy, z.ly}, di);
       dr = nyr;

@@ -431,8 +431,10 @@ NM_HD bool delta_steps(const DeviceView& v, DeltaState& st, int steps, EscapeVal
   int j = st.j, i = st.i;
   const int zlast = v.zlen - 1;
   const int stop = (v.N - i < steps) ? v.N : i + steps;
+  Dbl2 z = v.z[j];
   for (; i < stop; i++) {
-    const Dbl2 z = v.z[j];
+    // the next orbit element, loaded before the step's arithmetic
+    const Dbl2 zn = v.z[j < zlast ? j + 1 : zlast];
     double tr = add_(twice_(z.x), dr);
     double ti = add_(twice_(z.y), di);
     double nre = add_(sub_(mul_(tr, dr), mul_(ti, di)), st.er);
@@ -440,7 +442,7 @@ NM_HD bool delta_steps(const DeviceView& v, DeltaState& st, int steps, EscapeVal
     dr = nre;
     di = nim;
     j++;
-    const Dbl2 zn = v.z[j];
+    z = zn;
     double yr = add_(zn.x, dr), yi = add_(zn.y, di);
     double r2 = add_(mul_(yr, yr), mul_(yi, yi));
     if (above_bits(r2, v.bailout2)) {
@@ -456,6 +458,7 @@ NM_HD bool delta_steps(const DeviceView& v, DeltaState& st, int steps, EscapeVal
       dr = yr;
       di = yi;
       j = 0;
+      z = v.z[0];
     }
   }
   st.dr = dr;

@@ -32,8 +32,9 @@ NM_HD bool delta_xd_steps(const DeviceView& v, DeltaXDState& st, int steps, Esca
   const int zlast = v.zlen - 1;
   const int stop = (v.N - i < steps) ? v.N : i + steps;
   const XD bail2 = xd_of(v.bailout2);
+  Dbl2 z = v.z[j];
   for (; i < stop; i++) {
-    const Dbl2 z = v.z[j];
+    const Dbl2 zn = v.z[j < zlast ? j + 1 : zlast];  // loaded before the step's arithmetic
     const XD tr = xd_add(xd_twice(xd_of(z.x)), dr);
     const XD ti = xd_add(xd_twice(xd_of(z.y)), di);
     const XD nre = xd_add(xd_sub(xd_mul(tr, dr), xd_mul(ti, di)), st.er);
@@ -41,7 +42,7 @@ NM_HD bool delta_xd_steps(const DeviceView& v, DeltaXDState& st, int steps, Esca
     dr = nre;
     di = nim;
     j++;
-    const Dbl2 zn = v.z[j];
+    z = zn;
     const XD yr = xd_add(xd_of(zn.x), dr), yi = xd_add(xd_of(zn.y), di);
     const XD r2 = xd_add(xd_mul(yr, yr), xd_mul(yi, yi));
     if (xd_gt(r2, bail2)) {
@@ -59,6 +60,7 @@ NM_HD bool delta_xd_steps(const DeviceView& v, DeltaXDState& st, int steps, Esca
       dr = yr;
       di = yi;
       j = 0;
+      z = v.z[0];
     }
   }
   st.dr = dr;
@@ -124,13 +126,13 @@ NM_HD bool delta_guarded_steps(const DeviceView& v, DeltaState& st, int steps, E
   const int zlast = v.zlen - 1;
   const int stop = (v.N - i < steps) ? v.N : i + steps;
   handover = false;
+  Dbl2 z = v.z[j];
   for (; i < stop; i++) {
-    const Dbl2 z = v.z[j];
+    const Dbl2 zn = v.z[j < zlast ? j + 1 : zlast];  // loaded before the step's arithmetic
     const double tr = add_(twice_(z.x), dr);
     const double ti = add_(twice_(z.y), di);
     const double nre = add_(sub_(mul_(tr, dr), mul_(ti, di)), st.er);
     const double nim = add_(add_(mul_(tr, di), mul_(ti, dr)), st.ei);
-    const Dbl2 zn = v.z[j + 1];
     const double yr = add_(zn.x, nre), yi = add_(zn.y, nim);
     if (near_underflow(tr) || near_underflow(ti) || near_underflow(nre) || near_underflow(nim) ||
         near_underflow(yr) || near_underflow(yi)) {
@@ -140,6 +142,7 @@ NM_HD bool delta_guarded_steps(const DeviceView& v, DeltaState& st, int steps, E
     dr = nre;
     di = nim;
     j++;
+    z = zn;
     const double r2 = add_(mul_(yr, yr), mul_(yi, yi));
     if (above_bits(r2, v.bailout2)) {
       sm = smoothing_of(r2, v.log_bailout);
@@ -153,6 +156,7 @@ NM_HD bool delta_guarded_steps(const DeviceView& v, DeltaState& st, int steps, E
       dr = yr;
       di = yi;
       j = 0;
+      z = v.z[0];
     }
   }
   st.dr = dr;

@@ -193,10 +193,10 @@ def run_ours(args):
 
     primary = nm.PATH_FE32 if args.path == "fe32" else nm.PATH_FP64
     if args.profile:
-        # One render per path of a 1/div-size crop of the workload (same center
-        # and width, fewer samples): the case the ncu captures run on.
+        # One render per path of the central 1/div x 1/div crop of the workload
+        # (same center and sample step, fewer samples): the case the ncu
+        # captures run on.
         NR, NC = NR // args.profile, NC // args.profile
-        step = step_string_for(NC)
         for path in (nm.PATH_FE32, nm.PATH_FP64):
             mm = make(path)
             mm.precompute()

@@ -34,9 +34,11 @@ struct HwJob {
   }
 };
 
-// Views with a floatexp series front iterate in FP64 with an unbounded
-// exponent (pixel_xd.cuh); the rest in plain doubles.  The choice is per view,
-// so a warp of one view never diverges on it.
+// Views with a floatexp series front iterate in plain doubles while every
+// value stays clear of the underflow range and in FP64 with an unbounded
+// exponent (pixel_xd.cuh) otherwise, moving between the two at step (plain to
+// unbounded) and chunk (back) boundaries -- the results are the unbounded
+// form's throughout.  The other views iterate in plain doubles.
 struct Delta64Job {
   struct State {
     union {
@@ -71,6 +73,7 @@ struct Delta64Job {
       done = delta_steps(v, st.d, n, out, sm);
     } else if (st.xd) {
       done = delta_xd_steps(v, st.x, n, out, sm);
+      if (!done && delta_xd_to_plain(st.x, st.d)) st.xd = 0;
     } else {
       bool handover;
       done = delta_guarded_steps(v, st.d, n, out, sm, handover);

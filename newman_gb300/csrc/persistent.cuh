@@ -46,8 +46,157 @@ __device__ __forceinline__ void log_cost(const DeviceView& v, int r, int c,
   if (v.tile_cost && steps) atomicAdd(&v.tile_cost[tile_at(v, r, c)], steps * weight);
 }
 
+// ---- block-local compaction of FP64 samples ---------------------------------
+//
+// The FP64 pipe spends the same time on a warp instruction whatever the number
+// of its active lanes (on GB300 one FP64 warp instruction per 80 cycles of an
+// SM sub-partition, with 1 or 32 lanes active), so FP64 samples are best
+// carried in full warps.  Once the work a warp draws from has run dry, lanes
+// whose samples finish stay empty; then the warps of a block pool their
+// samples in shared memory (state, position and steps so far) so that fewer,
+// fuller warps carry them on:
+//   * a warp left with fewer than kCompactBelow samples hands them to the
+//     pool -- and, once no more work can arrive, leaves, when the block's
+//     other warps can hold every sample;
+//   * a warp with empty lanes takes samples from the pool: freely while it
+//     keeps running anyway (kCompactBelow samples or more), otherwise only
+//     when kCompactBelow samples wait there or no more work can arrive (so
+//     that a warp's few samples do not just come back to it);
+//   * a warp leaves only through the pool's lock, and never while samples
+//     wait in the pool with no other warp of the block left to take them.
+// One lock per block guards the pool (short critical sections, bounded spins;
+// a warp that cannot take it keeps its samples and tries again later).  The
+// order in which samples run does not change their results.
+
+constexpr int kPoolCap = 128;
+constexpr int kCompactBelow = 16;
+constexpr unsigned kPoolLockSpins = 1u << 12;
+
+template <class State>
+struct PoolEntry {
+  State st;
+  unsigned long long spent;  // steps run so far (the cost log's share)
+  int32_t f, r, c, pad_;
+};
+
+template <class State>
+struct SamplePool {
+  PoolEntry<State> e[kPoolCap];
+  int32_t count;  // waiting samples: e[0, count)
+  int32_t lock;
+  int32_t alive;  // warps of the block inside the loop
+  int32_t held;   // samples in those warps' lanes (as last reported)
+};
+
+// Every thread of the block calls it at the start of the kernel.
+template <class State>
+__device__ __forceinline__ void pool_init(SamplePool<State>* p) {
+  if (threadIdx.x == 0) {
+    p->count = 0;
+    p->lock = 0;
+    p->alive = 0;
+    p->held = 0;
+  }
+  __syncthreads();
+}
+
+template <class State>
+__device__ __forceinline__ void pool_enter(SamplePool<State>* p) {
+  if (p && (threadIdx.x & 31) == 0) atomicAdd(&p->alive, 1);
+}
+
+// One exchange with the pool by a full warp (every lane calls it).  `closed`:
+// no more work can arrive for this loop.  Returns true when the warp leaves.
+template <class Job>
+__device__ __forceinline__ bool pool_exchange(SamplePool<typename Job::State>* p, bool closed,
+                                              bool& active, typename Job::State& st,
+                                              unsigned long long executed,
+                                              unsigned long long& exec0, int& f, int& r, int& c,
+                                              int& held) {
+  const unsigned kFull = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  int ok = 0;
+  if (lane == 0) {
+    for (unsigned t = 0; t < kPoolLockSpins; t++) {
+      if (atomicCAS(&p->lock, 0, 1) == 0) {
+        ok = 1;
+        break;
+      }
+      __nanosleep(64);
+    }
+  }
+  if (!__shfl_sync(kFull, ok, 0)) return false;
+  __syncwarp();
+  int count = 0, alive = 0, held_all = 0;
+  if (lane == 0) {
+    count = *(volatile int32_t*)&p->count;
+    alive = *(volatile int32_t*)&p->alive;
+    held_all = *(volatile int32_t*)&p->held;
+  }
+  count = __shfl_sync(kFull, count, 0);
+  alive = __shfl_sync(kFull, alive, 0);
+  held_all = __shfl_sync(kFull, held_all, 0);
+  unsigned am = __ballot_sync(kFull, active);
+  int k = __popc(am);
+  bool leave = false;
+  // hand a few samples over
+  if (k > 0 && k < kCompactBelow && count + k <= kPoolCap &&
+      (!closed || (alive - 1) * 32 >= held_all - held + k + count)) {
+    if (active) {
+      PoolEntry<typename Job::State>& e = p->e[count + __popc(am & ((1u << lane) - 1))];
+      e.st = st;
+      e.spent = executed - exec0;
+      e.f = f;
+      e.r = r;
+      e.c = c;
+      active = false;
+    }
+    count += k;
+    k = 0;
+    am = 0;
+    leave = closed;
+    __syncwarp();
+  }
+  // fill empty lanes
+  if (!leave) {
+    const int idle = 32 - k;
+    int take = 0;
+    if (idle > 0 && count > 0 && (k >= kCompactBelow || closed || count >= kCompactBelow))
+      take = idle < count ? idle : count;
+    if (take > 0) {
+      const unsigned free_lanes = ~am;
+      const int rank = __popc(free_lanes & ((1u << lane) - 1));
+      if (!active && rank < take) {
+        const PoolEntry<typename Job::State>& e = p->e[count - take + rank];
+        st = e.st;
+        exec0 = executed - e.spent;
+        f = e.f;
+        r = e.r;
+        c = e.c;
+        active = true;
+      }
+      count -= take;
+      k += take;
+    }
+    if (k == 0 && closed && count == 0) leave = true;
+  }
+  __threadfence_block();
+  __syncwarp();
+  if (lane == 0) {
+    p->count = count;
+    p->held += (leave ? 0 : k) - held;
+    if (leave) p->alive -= 1;
+    __threadfence_block();
+    atomicExch(&p->lock, 0);
+  }
+  held = leave ? 0 : k;
+  __syncwarp();
+  return leave;
+}
+
 template <class Job, class Src>
-__device__ __forceinline__ void sample_loop(const Src& src, const RenderCtl& ctl, int chunk) {
+__device__ __forceinline__ void sample_loop(const Src& src, const RenderCtl& ctl, int chunk,
+                                            SamplePool<typename Job::State>* pool = nullptr) {
   const unsigned kFull = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   typename Job::State st;
@@ -57,6 +206,10 @@ __device__ __forceinline__ void sample_loop(const Src& src, const RenderCtl& ctl
   unsigned long long executed = 0, rebases = 0, finished = 0, undecided = 0, exec0 = 0;
   const unsigned long long end =
       ctl.count_ptr ? *ctl.count_ptr : (unsigned long long)ctl.count;
+  int held = 0;
+  unsigned naps = 0;
+  if (Job::kCertifies) pool = nullptr;  // a certifying job's samples carry their list index
+  pool_enter(pool);
 
   for (;;) {
     // Refill every idle lane (a new sample may finish at once, e.g. inside
@@ -96,7 +249,16 @@ __device__ __forceinline__ void sample_loop(const Src& src, const RenderCtl& ctl
         }
       }
     }
-    if (!__any_sync(kFull, active)) break;
+    if (pool && __any_sync(kFull, exhausted) &&
+        pool_exchange<Job>(pool, true, active, st, executed, exec0, f, r, c, held))
+      break;
+    if (!__any_sync(kFull, active)) {
+      // without a pool, or after leaving it, nothing is left; with one, its
+      // lock was busy: try again (bounded)
+      if (!pool || ++naps > kPoolLockSpins) break;
+      __nanosleep(1000);
+      continue;
+    }
     if (active) {
       EscapeValue out;
       double sm = 0.0;
@@ -130,8 +292,9 @@ __device__ __forceinline__ void sample_loop(const Src& src, const RenderCtl& ctl
 
 template <class Job>
 __device__ __forceinline__ void persistent_loop(const DeviceView& v, const RenderCtl& ctl,
-                                                int chunk) {
-  sample_loop<Job>(OneView{v}, ctl, chunk);
+                                                int chunk,
+                                                SamplePool<typename Job::State>* pool = nullptr) {
+  sample_loop<Job>(OneView{v}, ctl, chunk, pool);
 }
 
 // ---- a list that other warps of the same launch are still filling ----------
@@ -195,7 +358,8 @@ template <class Job, class Src>
 __device__ __forceinline__ void drain_loop(const Src& src, const RenderCtl& ctl,
                                            const unsigned long long* producers_done,
                                            unsigned long long producers,
-                                           unsigned long long* timeouts, int chunk) {
+                                           unsigned long long* timeouts, int chunk,
+                                           SamplePool<typename Job::State>* pool = nullptr) {
   const unsigned kFull = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   typename Job::State st;
@@ -203,8 +367,11 @@ __device__ __forceinline__ void drain_loop(const Src& src, const RenderCtl& ctl,
   int r = 0, c = 0, f = 0;
   unsigned idle = 0;
   unsigned long long executed = 0, rebases = 0, finished = 0, undecided = 0, lost = 0, exec0 = 0;
+  int held = 0;
+  pool_enter(pool);
   for (;;) {
     const unsigned need = __ballot_sync(kFull, !active);
+    bool dry = need != 0;  // empty lanes the list could not fill
     if (need && !closed) {
       const int leader = __ffs(need) - 1;
       unsigned long long base = 0;
@@ -226,6 +393,7 @@ __device__ __forceinline__ void drain_loop(const Src& src, const RenderCtl& ctl,
       status = __shfl_sync(kFull, status, leader);
       done = __shfl_sync(kFull, done, leader);
       if (done && status == CLAIM_EMPTY) closed = true;
+      dry = got < (unsigned)__popc(need);
       if (!active) {
         const unsigned rank = __popc(need & ((1u << lane) - 1));
         if (rank < got) {
@@ -248,8 +416,15 @@ __device__ __forceinline__ void drain_loop(const Src& src, const RenderCtl& ctl,
         }
       }
     }
+    // after kDrainIdlePolls idle polls the rest of the list is left to the
+    // next launch; samples waiting in the pool are still carried on here
+    const bool fin = closed || idle > kDrainIdlePolls;
+    if (pool && (dry || fin) &&
+        pool_exchange<Job>(pool, fin, active, st, executed, exec0, f, r, c, held))
+      break;
     if (!__any_sync(kFull, active)) {
-      if (closed || ++idle > kDrainIdlePolls) break;
+      if (!pool ? fin : idle > 2 * kDrainIdlePolls) break;
+      ++idle;
       __nanosleep(2000);
       continue;
     }

@@ -172,6 +172,24 @@ NM_HD bool delta_guarded_steps(const DeviceView& v, DeltaState& st, int steps, E
   return false;
 }
 
+// The unbounded-exponent state back in plain doubles, when each value is
+// exactly a double that the guarded steps accept: delta's components zero or
+// in [2^-400, 2^1000), eps's zero or normal.  (After a rebase delta is of the
+// order of the orbit again: the rest of a long sample runs in plain doubles.)
+NM_HD bool delta_xd_to_plain(const DeltaXDState& x, DeltaState& d) {
+  auto fits = [](const XD& a, int32_t lo) { return a.m == 0.0 || (a.e >= lo && a.e < 1000); };
+  if (!fits(x.dr, -400) || !fits(x.di, -400) || !fits(x.er, -1022) || !fits(x.ei, -1022))
+    return false;
+  const DeltaXDState c = x;  // x and d may share storage
+  d.dr = xd_to_double(c.dr);
+  d.di = xd_to_double(c.di);
+  d.er = xd_to_double(c.er);
+  d.ei = xd_to_double(c.ei);
+  d.j = c.j;
+  d.i = c.i;
+  return true;
+}
+
 NM_HD void delta_to_xd(const DeltaState& d, DeltaXDState& x) {
   const DeltaState c = d;  // d and x may share storage
   x.dr = xd_of(c.dr);

@@ -174,7 +174,9 @@ template <class Job>
 __global__ void __launch_bounds__(kPersistentThreads) batch_list_kernel(BatchGroup grp,
                                                                           RenderCtl ctl,
                                                                           int chunk) {
-  sample_loop<Job>(Frames{grp}, ctl, chunk);
+  __shared__ SamplePool<typename Job::State> pool;
+  pool_init(&pool);
+  sample_loop<Job>(Frames{grp}, ctl, chunk, &pool);
 }
 
 // The FE32 iteration of every FE32 frame with the FP64 work overlapped (the
@@ -190,22 +192,26 @@ __global__ void __launch_bounds__(kPersistentThreads) batch_list_kernel(BatchGro
 // then stays out of the FP32 iteration's allocation.
 __device__ __noinline__ void batch_fp64_side(const BatchGroup& fe, const BatchGroup& hw,
                                              const RenderCtl& hw_ctl, const OverlapCtl& o,
-                                             unsigned long long producers) {
+                                             unsigned long long producers,
+                                             SamplePool<Fp64AnyJob::State>* pool) {
   if (hw.n > 0) sample_loop<HwJob>(Frames{hw}, hw_ctl, o.chunk);
-  drain_loop<Fp64AnyJob>(Frames{fe}, o.rework, o.fe_warps_done, producers, o.timeouts, o.chunk);
+  drain_loop<Fp64AnyJob>(Frames{fe}, o.rework, o.fe_warps_done, producers, o.timeouts, o.chunk,
+                         pool);
 }
 
 template <int kFp64Warps>
 __global__ void __launch_bounds__(kPersistentThreads, 4)
     batch_overlap_kernel(BatchGroup fe, FePassBuffers b, RenderCtl fe_ctl, BatchGroup hw,
                          RenderCtl hw_ctl, OverlapCtl o, int chunk) {
+  __shared__ SamplePool<Fp64AnyJob::State> pool;
+  pool_init(&pool);
   const int warp = threadIdx.x >> 5;
   const int fe_warps = kPersistentThreads / 32 - kFp64Warps;
   if (warp < fe_warps) {
     batch_iter_warp(fe, b, fe_ctl, chunk);
     producer_warp_done(o.fe_warps_done);
   }
-  batch_fp64_side(fe, hw, hw_ctl, o, (unsigned long long)gridDim.x * fe_warps);
+  batch_fp64_side(fe, hw, hw_ctl, o, (unsigned long long)gridDim.x * fe_warps, &pool);
 }
 
 // Multisample mean of every frame (mandelbrot.cpp:320-332), float arithmetic

@@ -200,19 +200,23 @@ constexpr int kOverlapWarps = 2;
 // The FP64 side, out of line: its register pressure (the FP64 series front)
 // then stays out of the FP32 iteration's allocation.
 __device__ __noinline__ void overlap_fp64_side(const DeviceView& v, const OverlapCtl& o,
-                                               unsigned long long producers) {
-  drain_loop<Fp64AnyJob>(OneView{v}, o.rework, o.fe_warps_done, producers, o.timeouts, o.chunk);
+                                               unsigned long long producers,
+                                               SamplePool<Fp64AnyJob::State>* pool) {
+  drain_loop<Fp64AnyJob>(OneView{v}, o.rework, o.fe_warps_done, producers, o.timeouts, o.chunk,
+                         pool);
 }
 
 __global__ void __launch_bounds__(kPersistentThreads, 4) fe_overlap_kernel(
     DeviceView v, FePassBuffers b, RenderCtl ctl, OverlapCtl o, int chunk) {
+  __shared__ SamplePool<Fp64AnyJob::State> pool;
+  pool_init(&pool);
   const int warp = threadIdx.x >> 5;
   const int fe_warps = kPersistentThreads / 32 - kOverlapWarps;
   if (warp < fe_warps) {
     fe_iter_warp(v, b, ctl, chunk);
     producer_warp_done(o.fe_warps_done);
   }
-  overlap_fp64_side(v, o, (unsigned long long)gridDim.x * fe_warps);
+  overlap_fp64_side(v, o, (unsigned long long)gridDim.x * fe_warps, &pool);
 }
 
 int blocks_for(const void* kernel, int threads, int device) {

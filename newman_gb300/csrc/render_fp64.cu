@@ -12,17 +12,23 @@ namespace nmg {
 
 __global__ void __launch_bounds__(kPersistentThreads) hw_kernel(DeviceView v, RenderCtl ctl,
                                                                   int chunk) {
-  persistent_loop<HwJob>(v, ctl, chunk);
+  __shared__ SamplePool<HwJob::State> pool;
+  pool_init(&pool);
+  persistent_loop<HwJob>(v, ctl, chunk, &pool);
 }
 
 __global__ void __launch_bounds__(kPersistentThreads) delta64_kernel(DeviceView v, RenderCtl ctl,
                                                                        int chunk) {
-  persistent_loop<Delta64Job>(v, ctl, chunk);
+  __shared__ SamplePool<Delta64Job::State> pool;
+  pool_init(&pool);
+  persistent_loop<Delta64Job>(v, ctl, chunk, &pool);
 }
 
 __global__ void __launch_bounds__(kPersistentThreads) rework_kernel(DeviceView v, RenderCtl ctl,
                                                                       int chunk) {
-  persistent_loop<Fp64AnyJob>(v, ctl, chunk);
+  __shared__ SamplePool<Fp64AnyJob::State> pool;
+  pool_init(&pool);
+  persistent_loop<Fp64AnyJob>(v, ctl, chunk, &pool);
 }
 
 cudaError_t launch_fe32(const DeviceView& v, const RenderCtl& ctl, cudaStream_t stream,

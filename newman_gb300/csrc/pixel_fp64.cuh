@@ -404,8 +404,12 @@ NM_HD bool series_front(const DeviceView& v, int r, int c, SeriesFront& f, Escap
 // patterns, and |delta|^2 is formed only when |Y| is not clearly larger: 13
 // FP64 operations a step instead of 20, with the same results.
 struct DeltaState {
-  double dr, di, er, ei;
+  double dr, di, er, ei;  // er, ei: eps as the plain step adds it
   int32_t j, i;
+  // eps exactly, xr 2^xre + i xi 2^xie (floatexp views, where the plain step
+  // adds 0 for a component below the double range: eps_tiny)
+  double xr, xi;
+  int32_t xre, xie, eps_tiny;
 };
 
 NM_HD double scalbn_d(double x, int n) {
@@ -423,6 +427,10 @@ NM_HD void delta_start(const SeriesFront& f, DeltaState& st) {
   st.ei = scalbn_d(f.eps.im, f.eps_e);
   st.j = f.dsize;  // found + 1
   st.i = f.dsize;
+  st.xr = st.er;
+  st.xi = st.ei;
+  st.xre = st.xie = 0;
+  st.eps_tiny = 0;
 }
 
 NM_HD bool delta_steps(const DeviceView& v, DeltaState& st, int steps, EscapeValue& out,

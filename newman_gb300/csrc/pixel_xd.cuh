@@ -91,22 +91,40 @@ NM_HD bool near_underflow(double x) {
   return ((b >> 52) & 0x7ff) < 623 && (b & 0x7fffffffffffffffll) != 0;
 }
 
-// eps and d[found] of an FE front as plain doubles, when each is exactly
+// An eps component m 2^e for the plain step: the double itself when it is
+// zero or normal (exactly), else 0 with `tiny` set when it lies below the
+// double range -- it is then below half an ulp of every sum it is added to
+// while those sums are nonzero and at least 2^-400, which the guarded steps
+// check.  False beyond the double range.
+NM_HD bool plain_eps(double m, int32_t e, double& out, int32_t& tiny) {
+  const XD x = xd_of(m, e);
+  out = 0.0;
+  if (x.m == 0.0) return true;
+  if (x.e < -1022) {
+    tiny = 1;
+    return true;
+  }
+  if (x.e > 1000) return false;
+  out = xd_to_double(x);  // normal: exact
+  return true;
+}
+
+// eps and d[found] of an FE front as plain doubles, when delta is exactly
 // representable with room to spare (zero, or a normal double of at least
-// 2^-400 for delta; zero or normal for eps, which is only ever added).
+// 2^-400) and eps by plain_eps.
 NM_HD bool delta_plain_start(const SeriesFront& f, DeltaState& st) {
   const double dr = scalbn_d(f.dfound.re, f.d_e), di = scalbn_d(f.dfound.im, f.d_e);
-  const double er = scalbn_d(f.eps.re, f.eps_e), ei = scalbn_d(f.eps.im, f.eps_e);
   auto normal_or_zero = [](double x) {
     const int e = exp_field(x);
     return x == 0.0 || (e >= 1 && e <= 2045);
   };
-  if (near_underflow(dr) || near_underflow(di) || !normal_or_zero(dr) || !normal_or_zero(di) ||
-      !normal_or_zero(er) || !normal_or_zero(ei))
+  if (near_underflow(dr) || near_underflow(di) || !normal_or_zero(dr) || !normal_or_zero(di))
     return false;
   // the scalbn results are exact here: the FE mantissas carry 53 bits
-  if (scalbn_d(dr, -f.d_e) != f.dfound.re || scalbn_d(di, -f.d_e) != f.dfound.im ||
-      scalbn_d(er, -f.eps_e) != f.eps.re || scalbn_d(ei, -f.eps_e) != f.eps.im)
+  if (scalbn_d(dr, -f.d_e) != f.dfound.re || scalbn_d(di, -f.d_e) != f.dfound.im) return false;
+  double er, ei;
+  int32_t tiny = 0;
+  if (!plain_eps(f.eps.re, f.eps_e, er, tiny) || !plain_eps(f.eps.im, f.eps_e, ei, tiny))
     return false;
   st.dr = dr;
   st.di = di;
@@ -114,6 +132,10 @@ NM_HD bool delta_plain_start(const SeriesFront& f, DeltaState& st) {
   st.ei = ei;
   st.j = f.dsize;
   st.i = f.dsize;
+  st.xr = f.eps.re;
+  st.xi = f.eps.im;
+  st.xre = st.xie = f.eps_e;
+  st.eps_tiny = tiny;
   return true;
 }
 
@@ -125,6 +147,7 @@ NM_HD bool delta_guarded_steps(const DeviceView& v, DeltaState& st, int steps, E
   int j = st.j, i = st.i;
   const int zlast = v.zlen - 1;
   const int stop = (v.N - i < steps) ? v.N : i + steps;
+  const bool eps_tiny = st.eps_tiny != 0;
   handover = false;
   Dbl2 z = v.z[j];
   for (; i < stop; i++) {
@@ -134,8 +157,11 @@ NM_HD bool delta_guarded_steps(const DeviceView& v, DeltaState& st, int steps, E
     const double nre = add_(sub_(mul_(tr, dr), mul_(ti, di)), st.er);
     const double nim = add_(add_(mul_(tr, di), mul_(ti, dr)), st.ei);
     const double yr = add_(zn.x, nre), yi = add_(zn.y, nim);
+    // (with eps below the double range its components were not added: exact
+    // unless a sum came out 0)
     if (near_underflow(tr) || near_underflow(ti) || near_underflow(nre) || near_underflow(nim) ||
-        near_underflow(yr) || near_underflow(yi)) {
+        near_underflow(yr) || near_underflow(yi) ||
+        (eps_tiny && ((xd_bits_(nre) << 1) == 0 || (xd_bits_(nim) << 1) == 0))) {
       handover = true;  // state (dr, di, j, i) is before this step
       break;
     }
@@ -177,16 +203,24 @@ NM_HD bool delta_guarded_steps(const DeviceView& v, DeltaState& st, int steps, E
 // in [2^-400, 2^1000), eps's zero or normal.  (After a rebase delta is of the
 // order of the orbit again: the rest of a long sample runs in plain doubles.)
 NM_HD bool delta_xd_to_plain(const DeltaXDState& x, DeltaState& d) {
-  auto fits = [](const XD& a, int32_t lo) { return a.m == 0.0 || (a.e >= lo && a.e < 1000); };
-  if (!fits(x.dr, -400) || !fits(x.di, -400) || !fits(x.er, -1022) || !fits(x.ei, -1022))
-    return false;
   const DeltaXDState c = x;  // x and d may share storage
+  auto fits = [](const XD& a) { return a.m == 0.0 || (a.e >= -400 && a.e < 1000); };
+  double er, ei;
+  int32_t tiny = 0;
+  if (!fits(c.dr) || !fits(c.di) || !plain_eps(c.er.m, c.er.e, er, tiny) ||
+      !plain_eps(c.ei.m, c.ei.e, ei, tiny))
+    return false;
   d.dr = xd_to_double(c.dr);
   d.di = xd_to_double(c.di);
-  d.er = xd_to_double(c.er);
-  d.ei = xd_to_double(c.ei);
+  d.er = er;
+  d.ei = ei;
   d.j = c.j;
   d.i = c.i;
+  d.xr = c.er.m;
+  d.xi = c.ei.m;
+  d.xre = c.er.e;
+  d.xie = c.ei.e;
+  d.eps_tiny = tiny;
   return true;
 }
 
@@ -194,8 +228,8 @@ NM_HD void delta_to_xd(const DeltaState& d, DeltaXDState& x) {
   const DeltaState c = d;  // d and x may share storage
   x.dr = xd_of(c.dr);
   x.di = xd_of(c.di);
-  x.er = xd_of(c.er);
-  x.ei = xd_of(c.ei);
+  x.er = xd_of(c.xr, c.xre);
+  x.ei = xd_of(c.xi, c.xie);
   x.j = c.j;
   x.i = c.i;
 }

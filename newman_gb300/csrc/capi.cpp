@@ -42,6 +42,15 @@ constexpr unsigned long kDoubleLoopOrbitBits = 256;
 // path renders with the double loop directly -- the same escape counts.
 constexpr double kDoubleLoopFe32MinStep = 0x1p-33;
 
+// An upper bound on |c|_1 over the samples of the view (their coordinates as
+// the double loop takes them), as a float.
+float coord_abs_bound(const nm_handle* h) {
+  double mr = 0.0, mi = 0.0;
+  for (const Dbl2& x : h->coord_re) mr = std::max(mr, std::fabs(x.x) + std::fabs(x.y));
+  for (const Dbl2& y : h->coord_im) mi = std::max(mi, std::fabs(y.x) + std::fabs(y.y));
+  return std::nextafter((float)((mr + mi) * (1.0 + 0x1p-40)), INFINITY);
+}
+
 bool double_loop_direct(const nm_handle* h) {
   return h->path == NM_PATH_FE32 && h->view.use_hardware() &&
          h->view.step_max() < kDoubleLoopFe32MinStep;
@@ -305,6 +314,11 @@ int nmg::prepare_view(nm_handle* h, int r0, int r1, nmg::DeviceView& v, nmg::Ker
     v.sa_min = h->d_sa_min.p;
     set_fe_tables(h, v);
     v.double_loop = h->od.double_loop ? 1 : 0;
+    v.c_abs = coord_abs_bound(h);
+    if (h->od.double_loop) {  // the FE32 path on a double-loop view: trapping records
+      NM_CUDA(h->d_fe_trap.reserve((size_t)v.total));
+      v.trap = h->d_fe_trap.p;
+    }
   }
   v.grid = h->grid.p;
   v.smooth64 = h->keep_smooth64 ? h->smooth64.p : nullptr;
@@ -1003,6 +1017,7 @@ int noalloc_view(nm_handle* h, DeviceView& v, int& device, std::string& why, Ker
   v.sa_min = h->d_sa_min.p;
   set_fe_tables(h, v);
   v.double_loop = h->od.double_loop ? 1 : 0;
+  v.c_abs = coord_abs_bound(h);
   device = h->device;
   return NM_OK;
 }

@@ -52,6 +52,26 @@ constexpr float kFeUT = 0x1.61p-43f;
 // 2 (2^-20 (|Z| + |delta|) + e + u_z |Z| + u (|Z| + |delta|)), stays below
 // 2 (0.0043 + e + 2^-30) < 0.49 <= 1024 - |Y| whenever e < 0.2.
 constexpr float kFeQuickErr = 0.2f;
+
+// Interior orbits on double-loop views.  The reference's double loop F (one
+// step z -> z^2 + c in doubles, mandelbrot.cpp:242-246) rounds by at most
+//   |F(z) - f(z)| <= 2^-53 (3|z|^2 + |F(z)|_1) (1 + 2^-52),   f(z) = z^2 + c,
+// so for every double z in a disk D(w, r) around a point w of the exact orbit
+//   |F(z) - f(w)| <= r (2|w| + r) + 2^-52 (3.5 a^2 + 1.5 |c|_1),  a = |w| + r,
+// using |F(z)|_1 <= 1.5 (a^2 + |c|_1).  Following the image of a disk
+// B = D(P, R) along the exact orbit with this radius recurrence (rho), a
+// ball that comes back inside B after p steps traps the double loop: F^p(B)
+// lies in B and every intermediate image stays far inside the bailout, so a
+// double orbit that is in B never escapes and the double loop's result is N.
+// A disk is laid at each power-of-two iteration count from kTrapFirst on,
+// centred on the FE32 orbit point (float-float), with R = 16 times the
+// distance from there to the double orbit (the FE32 and double-loop bounds)
+// but at least 2^-36; the return is checked at the end of every chunk, and a
+// radius above kTrapRhoMax drops the disk.
+constexpr float kTrapRMin = 0x1p-36f;
+constexpr float kTrapRMax = 0x1p-20f;
+constexpr float kTrapRhoMax = 0x1p-4f;
+constexpr int kTrapFirst = 1024;
 constexpr float kFeBailout = 1024.0f;       // mandelbrot.cpp:58
 constexpr float kFeBailout2 = 1048576.0f;   // mandelbrot.cpp:59
 
@@ -455,16 +475,11 @@ __device__ __forceinline__ bool fe_scaled_steps(const DeviceView& v, FeState& st
 // certified with res filled, or uncertified (st.certified == 0), in which case
 // the iteration stops at once and res is not meaningful -- the sample goes to
 // the FP64 kernel.
-__device__ __forceinline__ bool fe_advance(const DeviceView& v, FeState& st, int steps,
-                                           FeResult& res, unsigned long long& executed,
-                                           unsigned long long& rebases) {
-  if (st.E != 0) {
-    if (v.double_loop) {  // a start below 2^-60: left to the double loop
-      st.certified = 0;
-      return true;
-    }
-    return fe_scaled_steps(v, st, steps, res, executed, rebases);
-  }
+// The unscaled steps; kDl: a double-loop view (second bound e64, trapping).
+template <bool kDl>
+__device__ __forceinline__ bool fe_unscaled_steps(const DeviceView& v, FeState& st, int steps,
+                                                  FeResult& res, unsigned long long& executed,
+                                                  unsigned long long& rebases, FeTrap* trap) {
   const int zlast = v.zlen - 1;
   const int stop = min(v.N, st.i + steps);
   const int start = st.i;
@@ -474,7 +489,9 @@ __device__ __forceinline__ bool fe_advance(const DeviceView& v, FeState& st, int
   FF dr = st.dr, di = st.di;
   float err = st.err;
   float e64 = st.e64;
-  const bool dloop = v.double_loop != 0;
+  constexpr bool dloop = kDl;
+  // the radius of the followed trapping disk's image (a sample starts at i = 0)
+  float rho = (kDl && trap && st.i > 0) ? trap->rho : 0.0f;
   int j = st.j, i = st.i;
   bool certified = st.certified != 0;
   ZFF z = fe_load_z(v, j);
@@ -524,6 +541,14 @@ __device__ __forceinline__ bool fe_advance(const DeviceView& v, FeState& st, int
         const float l64 = up_mul(0x1p-52f, up_fma(up_mul(2.0f, z_old), z_old, z_new));
         e64 = up_fma(up_fma(2.0f, w_old, e64), e64, l64);
         yerr = up_add(yerr, up_fma(0x1p-52f, z_new, e64));
+        if (rho > 0.0f) {  // the image of the trapping disk around the exact orbit
+          const float a = up_add(w_old, rho);
+          const float l64r = up_mul(0x1p-52f, up_fma(up_mul(3.5f, a), a, up_mul(1.5f, v.c_abs)));
+          rho = up_fma(up_fma(2.0f, w_old, rho), rho, l64r);
+          // dropped where the disk's image could reach the bailout or grow past
+          // the linear regime
+          if (!(up_add(rho, err) <= kTrapRhoMax) || !(r2 <= lo_band)) rho = 0.0f;
+        }
       }
       if (r2 <= lo_band) {
         // |Y| is below the bailout by more than 2^-11 of it; the estimate ym
@@ -566,6 +591,42 @@ __device__ __forceinline__ bool fe_advance(const DeviceView& v, FeState& st, int
       rebases++;
     }
   }
+  if (kDl && trap && !done && certified && i < v.N) {
+    // P: the FE32 orbit point Y = Z + delta in float-float, to mgn of Y; the
+    // exact orbit within cerr of Y, the double loop's within e64 of it
+    const float zn1 = up_add(fabsf(z.hx), fabsf(z.hy)), dn1 = up_add(fabsf(dr.h), fabsf(di.h));
+    const FF px = ff_add(FF{z.hx, z.lx}, dr), py = ff_add(FF{z.hy, z.ly}, di);
+    const float mgn = up_mul(0x1p-43f, up_add(zn1, dn1));
+    const float cerr = up_add(err, up_mul(kFeUZ, zn1));
+    if (rho > 0.0f) {
+      // back inside: D(exact orbit, rho) within the disk D(P_saved, R)
+      const FF ddx = ff_add(px, FF{-trap->pxh, -trap->pxl});
+      const FF ddy = ff_add(py, FF{-trap->pyh, -trap->pyl});
+      const float dist = up_add(up_add(up_add(fabsf(ddx.h), fabsf(ddx.l)),
+                                       up_add(fabsf(ddy.h), fabsf(ddy.l))),
+                                up_mul(0x1p-43f, up_add(up_add(zn1, dn1), up_add(
+                                    fabsf(trap->pxh), fabsf(trap->pyh)))));
+      if (up_add(up_add(dist, up_add(mgn, cerr)), rho) <= trap->R) {
+        done = true;
+        res.it = v.N;
+        res.r2 = FF{0.f, 0.f};
+      }
+    }
+    // a new disk at each power of two from kTrapFirst on, when the double
+    // orbit lies well inside it: D(exact orbit, rho) covers D(P, R)
+    if (!done && i >= kTrapFirst && __clz(i) < __clz(start > 0 ? start : 1)) {
+      const float R = fmaxf(kTrapRMin, up_mul(16.0f, up_add(up_add(cerr, e64), mgn)));
+      if (R <= kTrapRMax) {
+        trap->pxh = px.h;
+        trap->pxl = px.l;
+        trap->pyh = py.h;
+        trap->pyl = py.l;
+        trap->R = R;
+        rho = up_add(up_add(R, mgn), cerr);
+      }
+    }
+    trap->rho = rho;
+  }
   executed += (unsigned long long)(i - start);
   st.dr = dr;
   st.di = di;
@@ -581,6 +642,20 @@ __device__ __forceinline__ bool fe_advance(const DeviceView& v, FeState& st, int
     return true;
   }
   return false;
+}
+
+__device__ __forceinline__ bool fe_advance(const DeviceView& v, FeState& st, int steps,
+                                           FeResult& res, unsigned long long& executed,
+                                           unsigned long long& rebases, FeTrap* trap = nullptr) {
+  if (st.E != 0) {
+    if (v.double_loop) {  // a start below 2^-60: left to the double loop
+      st.certified = 0;
+      return true;
+    }
+    return fe_scaled_steps(v, st, steps, res, executed, rebases);
+  }
+  if (v.double_loop) return fe_unscaled_steps<true>(v, st, steps, res, executed, rebases, trap);
+  return fe_unscaled_steps<false>(v, st, steps, res, executed, rebases, nullptr);
 }
 
 }  // namespace nmg

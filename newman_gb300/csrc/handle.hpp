@@ -122,6 +122,7 @@ struct nm_handle {
   bool fe_single_pass = false;  // FE32 in one persistent kernel instead of the passes
   bool fe_overlap = true;       // FE32 passes: FP64 rework inside the iteration pass
   DevBuf<char> d_fe_state;
+  DevBuf<nmg::FeTrap> d_fe_trap;  // double-loop views on the FE32 path
   DevBuf<unsigned int> d_work;
 
   // scheduling: the order in which whole-grid renders hand out their tiles (a

@@ -133,7 +133,8 @@ __device__ __forceinline__ void batch_iter_warp(const BatchGroup& grp, const FeP
     if (active) {
       FeResult res;
       const DeviceView& v = grp.views[f];
-      if (fe_advance(v, st, chunk, res, executed, rebases)) {
+      if (fe_advance(v, st, chunk, res, executed, rebases,
+                     v.trap ? v.trap + (g - grp.offsets[f]) : nullptr)) {
         int r = 0, c = 0;
         sample_rc(v, g - grp.offsets[f], r, c);
         log_cost(v, r, c, executed - exec0, 1);

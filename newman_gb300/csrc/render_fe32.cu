@@ -154,7 +154,7 @@ __device__ __forceinline__ void fe_iter_warp(const DeviceView& v, const FePassBu
     if (!__any_sync(kFull, active)) break;
     if (active) {
       FeResult res;
-      if (fe_advance(v, st, chunk, res, executed, rebases)) {
+      if (fe_advance(v, st, chunk, res, executed, rebases, v.trap ? v.trap + sid : nullptr)) {
         int r = 0, c = 0;
         sample_rc(v, sid, r, c);
         if (st.certified) {

@@ -28,6 +28,15 @@ struct alignas(16) Flt4 {
   float x, y, z, w;
 };
 
+// Per-sample record of the interior-orbit trapping on double-loop views
+// (fe_core.cuh): the center P of the trapping disk in float-float, its radius
+// R, and the radius rho of its image around the exact orbit (0: none).
+struct alignas(16) FeTrap {
+  float pxh, pxl, pyh, pyl;
+  float rho, R;
+  int32_t pad_[2];
+};
+
 // Floatexp values: FP64 mantissas with an int exponent.
 struct CFE {  // (re + i im) * 2^e
   double re, im;
@@ -91,6 +100,8 @@ struct DeviceView {
   int32_t sa_fe;           // 1: eps, series and thresholds in floatexp (tables below)
   int32_t double_loop;     // 1: FE32 path certified against the double loop (no series;
                            //    eps = get_d(get_d(pt) - X[0]), orbit at the view center)
+  float c_abs;             // double-loop views: |c|_1 <= c_abs for every sample c
+  FeTrap* trap;            // double-loop views: one record per sample (tile order), or null
   const RFE* eps_re_fe;    // [nc]
   const RFE* eps_im_fe;    // [nr]
   const CFE* sa_a_fe;      // [xlen]

@@ -299,6 +299,7 @@ int nmg::prepare_view(nm_handle* h, int r0, int r1, nmg::DeviceView& v, nmg::Ker
   v.total = (long long)v.tiles_x * v.tiles_y * h->tile_w * h->tile_h;
   v.coord_re = h->d_coord_re.p;
   v.coord_im = h->d_coord_im.p;
+  v.c_abs = coord_abs_bound(h);
   if (!hw) {
     v.eps_re = h->d_eps_re.p;
     v.eps_im = h->d_eps_im.p;
@@ -314,7 +315,6 @@ int nmg::prepare_view(nm_handle* h, int r0, int r1, nmg::DeviceView& v, nmg::Ker
     v.sa_min = h->d_sa_min.p;
     set_fe_tables(h, v);
     v.double_loop = h->od.double_loop ? 1 : 0;
-    v.c_abs = coord_abs_bound(h);
     if (h->od.double_loop) {  // the FE32 path on a double-loop view: trapping records
       NM_CUDA(h->d_fe_trap.reserve((size_t)v.total));
       v.trap = h->d_fe_trap.p;

@@ -100,7 +100,7 @@ struct DeviceView {
   int32_t sa_fe;           // 1: eps, series and thresholds in floatexp (tables below)
   int32_t double_loop;     // 1: FE32 path certified against the double loop (no series;
                            //    eps = get_d(get_d(pt) - X[0]), orbit at the view center)
-  float c_abs;             // double-loop views: |c|_1 <= c_abs for every sample c
+  float c_abs;             // |c|_1 <= c_abs for every sample c (as the double loop takes it)
   FeTrap* trap;            // double-loop views: one record per sample (tile order), or null
   const RFE* eps_re_fe;    // [nc]
   const RFE* eps_im_fe;    // [nr]

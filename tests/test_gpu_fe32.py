@@ -105,3 +105,25 @@ def test_fe32_on_double_loop_views_matches_the_double_loop(nm, view):
     assert fe.stat(nm.STAT_SAMPLES) == fe.rows() * fe.cols()
     d = np.abs(ref.smoothing64()[same] - fe.smoothing64()[same])
     assert d.size == 0 or np.median(d) < 1e-6
+
+
+def test_fe32_traps_interior_orbits_of_double_loop_views(nm):
+    """A double-loop view inside the minibrot next to the C2 center (the C4
+    zoom's frame 8, at its sample step): the FE32 path proves most interior
+    orbits trapped long before N (a small disk that the double loop maps back
+    into itself) and returns the double loop's escape counts on every sample."""
+    view = dict(nr=128, nc=192, sc=1, cre="-0.743643899077151", cim="0.13182583196533",
+                step="3.0e-10", N=17703, tol=1e-10)
+    ref = setup_gpu(nm, view)
+    assert ref.useHardware()
+    ref.render()
+    fe = setup_gpu(nm, view, path=nm.PATH_FE32)
+    fe.precompute()
+    fe.render()
+    a, b = ref.grid()["iterations"], fe.grid()["iterations"]
+    interior = a >= view["N"]
+    print("interior %.3f, executed FE32 %d, double loop %d" % (
+        interior.mean(), fe.stat(nm.STAT_EXECUTED_ITERS), ref.stat(nm.STAT_EXECUTED_ITERS)))
+    assert interior.mean() > 0.5
+    assert np.array_equal(a, b)
+    assert fe.stat(nm.STAT_EXECUTED_ITERS) < 0.75 * ref.stat(nm.STAT_EXECUTED_ITERS)

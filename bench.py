@@ -121,6 +121,24 @@ def dist_setup():
     return world, rank, local
 
 
+def max_over_ranks(ms, device=None):
+    """The largest of every rank's step time (the job is as slow as its
+    slowest replica); the value itself with one rank."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(ms)
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(units_per_replica, world, ms):
+    """Whole-job throughput of `world` independent replicas, each processing
+    units_per_replica in a step of ms (the slowest rank's) milliseconds."""
+    return units_per_replica * world / (ms * 1e-3)
+
+
 def cpu_reference(seconds, threads, seed=7):
     """The reference algorithm on the host: getIterations with its
     arbitrary-precision continuation, on a seeded random sample of the
@@ -239,11 +257,7 @@ def run_ours(args):
         torch.cuda.synchronize()
         wall = time.perf_counter() - wall0
     barrier()
-    ms = float(np.mean(times))
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(float(np.mean(times)), device="cuda")
     g = m.grid()
     eff_iters = int(g["iterations"].astype(np.int64).sum())
     executed = m.stat(nm.STAT_EXECUTED_ITERS)
@@ -252,7 +266,7 @@ def run_ours(args):
     k_main_ms = m.stat(nm.STAT_KERNEL_NS) * 1e-6
     k_rework_ms = m.stat(nm.STAT_REWORK_KERNEL_NS) * 1e-6
     k_iter_ms = m.stat(nm.STAT_ITER_KERNEL_NS) * 1e-6
-    value = eff_iters * world / (ms * 1e-3)
+    value = replica_value(eff_iters, world, ms)
 
     # the plain FP64 path: timed on the same workload, and the comparison grid
     fp64_ms = None

@@ -133,6 +133,25 @@ def max_over_ranks(ms, device=None):
     return float(t.item())
 
 
+INSTR_PER_ITER = 128.7  # FE32 step: 5.30e12 thread instructions for 4.12e10 steps (ncu)
+
+
+def issue_roofline(executed, iter_ms, clocks):
+    """Thread instructions per second of the FE32 iteration pass against the
+    GPU's issue peak (4 x 32 lanes per SM per clock)."""
+    import torch
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    mhz = (clocks or {}).get("sm_mhz") or (clocks or {}).get("sm_max_mhz")
+    if not mhz or not iter_ms:
+        return None
+    achieved = executed * INSTR_PER_ITER / (iter_ms * 1e-3)
+    peak = 4 * 32 * sms * mhz * 1e6
+    return {"achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "T thread-instr/s",
+            "frac": achieved / peak, "instr_per_iter": INSTR_PER_ITER,
+            "note": "FE32 steps of the iteration pass (the overlapped FP64 rework's "
+                    "instructions are not counted); inactive lanes count as lost issue"}
+
+
 def replica_value(units_per_replica, world, ms):
     """Whole-job throughput of `world` independent replicas, each processing
     units_per_replica in a step of ms (the slowest rank's) milliseconds."""
@@ -333,7 +352,13 @@ def run_ours(args):
                          "frac": achieved / peak, "traffic": None,
                          "flops_per_iter": FLOPS_PER_ITER,
                          "peak_source": "measured by nm_peak_flops on this GPU "
-                                        "(FP32 FMA / FP64 unfused mul+add issue rate)"},
+                                        "(FP32 FMA / FP64 unfused mul+add issue rate)",
+                         # the limit that binds: instruction issue.  A float-float
+                         # step executes INSTR_PER_ITER thread instructions (ncu,
+                         # FE32 warps alone on the C2 view); peak = 4 schedulers x
+                         # 32 lanes x SMs x the SM clock sampled during the run
+                         "issue": None if primary != nm.PATH_FE32 else issue_roofline(
+                             executed, k_iter_ms, clocks.summary())},
             "clocks": clocks.summary(),
             "e2e": {"value": eff_iters / e2e_s, "unit": "pixel-iters/s",
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": NR * NC * 8},

@@ -37,8 +37,9 @@ constexpr unsigned long kDoubleLoopOrbitBits = 256;
 
 // The FE32 path on a double-loop view certifies against the double loop's own
 // rounding, which grows with the zoom: below a sample step of 2^-33 most
-// samples cannot be certified (measured on the C4 zoom: reworked fraction 7 %
-// at step 6e-10, 24 % at 1e-10, over 90 % below 1e-13), so there the FE32
+// samples cannot be certified (measured on a 1280x720 zoom into
+// -0.743643887037151+0.131825904205330i: reworked fraction 7 % at step 6e-10,
+// 24 % at 1e-10, over 90 % below 1e-13), so there the FE32
 // path renders with the double loop directly -- the same escape counts.
 constexpr double kDoubleLoopFe32MinStep = 0x1p-33;
 

@@ -66,9 +66,10 @@ constexpr float kFeQuickErr = 0.2f;
 // A disk is laid at each power-of-two iteration count from kTrapFirst on,
 // centred on the FE32 orbit point (float-float), with R = 16 times the
 // distance from there to the double orbit (the FE32 and double-loop bounds)
-// but at least 2^-22 (on the C4 zoom's double-loop frames 2^-22 traps the
-// most interior samples soonest: 2^-36 and 2^-18 took 1.5x and 1.4x as many
-// steps); the return is checked at the end of every chunk, and a radius
+// but at least 2^-22 (on the double-loop frames of a 240-frame 1280x720 zoom
+// into -0.743643887037151+0.131825904205330i, 2^-22 traps the most interior
+// samples soonest: 2^-36 and 2^-18 took 1.5x and 1.4x as many steps); the
+// return is checked at the end of every chunk, and a radius
 // above kTrapRhoMax drops the disk.
 constexpr float kTrapRMin = 0x1p-22f;
 constexpr float kTrapRMax = 0x1p-20f;

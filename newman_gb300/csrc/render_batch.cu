@@ -186,8 +186,9 @@ __global__ void __launch_bounds__(kPersistentThreads) batch_list_kernel(BatchGro
 // uncertified FE32 samples as they are appended; the other warps iterate in
 // FP32 and, when the FP32 work list is exhausted, join the FP64 side.  Capped
 // at 64 registers so that 4 blocks fit on an SM.  The split follows the
-// batch's FP64 work: on the 240-frame C4 zoom (7 double-loop frames) 4 FP64
-// warps of 8 give 1,819 ms, 6 give 1,862 ms, 2 give 2,030 ms (two runs each).
+// batch's FP64 work: on a 240-frame 1280x720 (2x2 samples) zoom from width 4
+// to 1e-200 with 7 double-loop frames, 4 FP64 warps of 8 gave 1,819 ms, 6 gave
+// 1,862 ms, 2 gave 2,030 ms (two runs each).
 
 // The FP64 side, out of line: its register pressure (the FP64 series front)
 // then stays out of the FP32 iteration's allocation.

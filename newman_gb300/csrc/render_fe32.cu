@@ -192,9 +192,10 @@ __global__ void __launch_bounds__(kPersistentThreads) fe_iter_kernel(DeviceView 
 // every block render uncertified samples in FP64 (the FP64 pipe is idle under
 // the FP32 iteration) from the start; the other warps iterate in FP32 and,
 // when the FP32 work list is exhausted, join the FP64 side.  Capped at 64
-// registers so that 4 blocks fit on an SM.  On the C2 view (2.7 % of the
-// samples reworked): 216 ms with two FP64 warps a block, 262 ms with one,
-// 231 ms with three, 273 ms with the rework after the pass.
+// registers so that 4 blocks fit on an SM.  On the 1920x1080 (4x4 samples)
+// view of width 1e-12, N 50,000 (2.7 % of the samples reworked): 191 ms with
+// two FP64 warps a block, 245 ms with one, 221 ms with three, 243 ms with the
+// rework after the pass.
 constexpr int kOverlapWarps = 2;
 
 // The FP64 side, out of line: its register pressure (the FP64 series front)

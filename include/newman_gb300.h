@@ -254,7 +254,9 @@ int nm_batch_get_stat(nm_batch* b, int stat, long long* value);
 int nm_batch_frames(nm_batch* b, nm_escape_value* host_out);
 /* Times every tile shape (8x8 .. 64x64) and FE32 renormalisation interval
    (8 .. 256) on every stride-th frame and keeps the fastest, then the FP64
-   side's share of the FE32 pass (NM_OPT_BATCH_FP64_WARPS 2, 4, 6). */
+   side's share of the FE32 pass (NM_OPT_BATCH_FP64_WARPS 2, 4, 6); last, the
+   result against the batch's own settings on the whole batch, keeping the
+   faster (a sub-batch can miss the few frames that dominate the batch). */
 int nm_batch_autotune(nm_batch* b, int stride, int* tile_w, int* tile_h, int* renorm);
 
 /* Render the handle's view on the FP32-floatexp path into device memory the

@@ -344,6 +344,7 @@ int nm_batch_frames(nm_batch* b, nm_escape_value* host_out) {
 int nm_batch_autotune(nm_batch* b, int stride, int* tile_w, int* tile_h, int* renorm) {
   if (!b || stride < 1) return fail(NM_ERR_ARG, "bad autotune arguments");
   if (b->frames.empty()) return fail(NM_ERR_STATE, "empty batch");
+  const int ow = b->tile_w, oh = b->tile_h, orn = b->fe_chunk, ofw = b->fp64_warps;
   // a sub-batch of every stride-th frame, same options
   nm_batch sub;
   sub.sc = b->sc;
@@ -401,16 +402,45 @@ int nm_batch_autotune(nm_batch* b, int stride, int* tile_w, int* tile_h, int* re
       }
     }
   }
-  b->tile_w = bw;
-  b->tile_h = bh;
-  b->fe_chunk = br;
-  b->fp64_warps = bfw;
-  b->invalidate();
-  // frames were prepared with the sub-batch's last tile shape: rebuild later
-  for (nm_handle* h : b->frames) {
-    h->tile_w = bw;
-    h->tile_h = bh;
+  // Last, the tuned settings against the batch's own on the whole batch (a
+  // sub-batch can miss the few frames that dominate it): the faster stays.
+  auto set = [&](int tw, int th, int rn, int fw) {
+    b->tile_w = tw;
+    b->tile_h = th;
+    b->fe_chunk = rn;
+    b->fp64_warps = fw;
+    b->invalidate();
+    // frames are prepared with the batch's tile shape when it is built
+    for (nm_handle* h : b->frames) {
+      h->tile_w = tw;
+      h->tile_h = th;
+    }
+  };
+  auto time_whole = [&](float& out) -> int {
+    if (int rc = nm_batch_render(b)) return rc;  // builds and warms up
+    out = 0.f;
+    for (int rep = 0; rep < 2; rep++) {
+      if (int rc = nm_batch_render(b)) return rc;
+      float m = 0.f;
+      NM_CUDA(cudaEventElapsedTime(&m, b->ev0, b->ev1));
+      out += m;
+    }
+    return NM_OK;
+  };
+  if (bw != ow || bh != oh || br != orn || bfw != ofw) {
+    float t_tuned = 0.f, t_own = 0.f;
+    set(bw, bh, br, bfw);
+    if (int rc = time_whole(t_tuned)) return rc;
+    set(ow, oh, orn, ofw);
+    if (int rc = time_whole(t_own)) return rc;
+    if (t_own <= t_tuned) {
+      bw = ow;
+      bh = oh;
+      br = orn;
+      bfw = ofw;
+    }
   }
+  set(bw, bh, br, bfw);
   if (tile_w) *tile_w = bw;
   if (tile_h) *tile_h = bh;
   if (renorm) *renorm = br;

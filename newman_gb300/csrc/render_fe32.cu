@@ -190,12 +190,14 @@ __global__ void __launch_bounds__(kPersistentThreads) fe_iter_kernel(DeviceView 
 
 // The iteration pass with the FP64 rework overlapped: the last two warps of
 // every block render uncertified samples in FP64 (the FP64 pipe is idle under
-// the FP32 iteration) from the start; the other warps iterate in FP32 and,
-// when the FP32 work list is exhausted, join the FP64 side.  Capped at 64
-// registers so that 4 blocks fit on an SM.  On the 1920x1080 (4x4 samples)
-// view of width 1e-12, N 50,000 (2.7 % of the samples reworked): 191 ms with
-// two FP64 warps a block, 245 ms with one, 221 ms with three, 243 ms with the
-// rework after the pass.
+// the FP32 iteration) from the start and drain the list to its end; the other
+// warps iterate in FP32 and leave when the FP32 work list is exhausted (the
+// FP64 code under this kernel's 64-register cap spills; a warp joining it
+// made a 3840x2160 (2x2) view of width 1e-413 5 % slower and helped nowhere).
+// Capped at 64 registers so that 4 blocks fit on an SM.  On the 1920x1080
+// (4x4 samples) view of width 1e-12, N 50,000 (2.7 % of the samples
+// reworked): 191 ms with two FP64 warps a block, 245 ms with one, 221 ms with
+// three, 243 ms with the rework after the pass.
 constexpr int kOverlapWarps = 2;
 
 // The FP64 side, out of line: its register pressure (the FP64 series front)
@@ -216,6 +218,7 @@ __global__ void __launch_bounds__(kPersistentThreads, 4) fe_overlap_kernel(
   if (warp < fe_warps) {
     fe_iter_warp(v, b, ctl, chunk);
     producer_warp_done(o.fe_warps_done);
+    return;
   }
   overlap_fp64_side(v, o, (unsigned long long)gridDim.x * fe_warps, &pool);
 }

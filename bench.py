@@ -158,6 +158,38 @@ def replica_value(units_per_replica, world, ms):
     return units_per_replica * world / (ms * 1e-3)
 
 
+def c1_double_loop(nm):
+    """The 640x480 view at -0.75+0i, width 3, N 1024, where the reference
+    takes its double loop (getIterationsHW): the GPU's double loop (device
+    time, 3 renders after a warm-up) against the oracle's restatement of the
+    reference on the whole frame, one thread and all host threads; the escape
+    counts must agree everywhere."""
+    from oracle import oracle
+    nr, nc, N, step = 480, 640, 1024, "0.0046875"
+    m = nm.Mandelbrot(nr, nc)
+    m.set_view("-0.75", "0", step, step, N, TOL)
+    m.set_path(nm.PATH_REFERENCE)
+    m.precompute()
+    m.render()
+    gpu = []
+    for _ in range(3):
+        m.render()
+        gpu.append(m.stat(nm.STAT_KERNEL_NS) * 1e-6)
+    g = m.grid()["iterations"]
+    out = {"samples": nr * nc, "effective_iters": int(g.astype(np.int64).sum()),
+           "gpu_ms": min(gpu)}
+    for label, threads in (("cpu_ms_1_thread", 1), ("cpu_ms_all_threads", os.cpu_count() or 1)):
+        o = oracle.OracleView(nr, nc)
+        o.set_view("-0.75", "0", step, step, N, TOL)
+        o.precompute(threads=threads)
+        t0 = time.perf_counter()
+        it, _ = o.render_rows(0, nr, threads=threads)
+        out[label] = (time.perf_counter() - t0) * 1e3
+        out["identical"] = bool(np.array_equal(it, g))
+    out["cores"] = os.cpu_count() or 1
+    return out
+
+
 def cpu_reference(seconds, threads, seed=7):
     """The reference algorithm on the host: getIterations with its
     arbitrary-precision continuation, on a seeded random sample of the
@@ -369,6 +401,7 @@ def run_ours(args):
                                     "kind": "port",
                                     "sample": "%d random samples of the 33,177,600, reference "
                                               "getIterations (MP continuation), 1 thread" % px}
+            line["c1_double_loop"] = c1_double_loop(nm)
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

@@ -61,7 +61,8 @@ enum nm_option {
   NM_OPT_KEEP_SMOOTH64 = 3, /* 1: also keep the unrounded double smoothing */
   NM_OPT_THREADS = 4,     /* host threads for the probe search (0 = all) */
   NM_OPT_BLOCKS = 5,      /* persistent blocks (0 = fill the GPU) */
-  NM_OPT_RENORM = 6,      /* FE32: steps between exponent renormalisations */
+  NM_OPT_RENORM = 6,      /* FE32: steps between exponent renormalisations (0: 64,
+                             32 on views below the double range) */
   NM_OPT_FE32_SINGLE_PASS = 7, /* FE32 in one persistent kernel (default: three passes) */
   NM_OPT_REFERENCE = 8,   /* reference orbit: 0 the reference's probe search
                              (findProbe, mandelbrot.cpp:73-95), 1 the view center */

@@ -488,7 +488,7 @@ int nm_set_option(nm_handle* h, int opt, long long value) {
       h->blocks = (int)value;
       return NM_OK;
     case NM_OPT_RENORM:
-      if (value < 1 || value > 256) return fail(NM_ERR_ARG, "renorm interval %lld", value);
+      if (value < 0 || value > 256) return fail(NM_ERR_ARG, "renorm interval %lld", value);
       h->renorm = (int)value;
       return NM_OK;
     case NM_OPT_FE32_SINGLE_PASS:
@@ -643,7 +643,8 @@ int nm_render_rows(nm_handle* h, int r0, int r1, void* stream_arg) {
   if (blocks > need_blocks) blocks = (int)need_blocks;
   if (blocks < 1) blocks = 1;
   int chunk = h->chunk;
-  if (kind == nmg::KERNEL_FE32) chunk = h->renorm;  // the FE32 kernel renormalises per chunk
+  if (kind == nmg::KERNEL_FE32)  // the FE32 kernel renormalises per chunk
+    chunk = h->renorm > 0 ? h->renorm : (v.sa_fe ? 32 : 64);
   NM_CUDA(cudaEventRecord(h->ev[0], s));
   h->timed_iter = false;
   if (kind == nmg::KERNEL_FE32 && !h->fe_single_pass) {

@@ -54,6 +54,13 @@ def test_bad_arguments_raise():
         m.set_view("0", "0", "1e-20", "1e-20", 100)
         m.render_rows(0, 4)  # deep view without precompute
     assert e.value.code == nm.NM_ERR_STATE
+    # FE32 chunk length: 0 picks the default, 1..256 explicit, anything else an error
+    for ok in (0, 1, 64, 256):
+        m.set_option(nm.OPT_RENORM, ok)
+    for bad in (-1, 257):
+        with pytest.raises(nm.NewmanError) as e:
+            m.set_option(nm.OPT_RENORM, bad)
+        assert e.value.code == nm.NM_ERR_ARG
 
 
 @pytest.mark.parametrize("shape,N", [((48, 64), 3000), ((27, 31), 8000)])

@@ -70,3 +70,103 @@ def test_float_float_t_bound():
         dh, dl = _ff_of(d)
         th, _ = _ff_add(2.0 * zh, 2.0 * zl, dh, dl)
         assert abs(float(th)) <= (2.0 * abs(float(zh)) + abs(float(dh))) * limit
+
+
+# ---- the float-float complex multiply-add of the FE32 step ----------------------
+
+def _rn32(q):
+    """q (a Fraction) rounded to the nearest float32, ties to even (normal range)."""
+    if q == 0:
+        return Q(0)
+    sign = -1 if q < 0 else 1
+    a = abs(q)
+    e = a.numerator.bit_length() - a.denominator.bit_length()
+    if Q(2) ** e > a:
+        e -= 1
+    scale = Q(2) ** (23 - e)  # a * scale in [2^23, 2^24)
+    m = a * scale
+    fl = m.numerator // m.denominator
+    rem = m - fl
+    if rem > Q(1, 2) or (rem == Q(1, 2) and fl % 2 == 1):
+        fl += 1
+    return sign * Q(fl) / scale
+
+
+def _add(a, b):
+    return _rn32(a + b)
+
+
+def _mul(a, b):
+    return _rn32(a * b)
+
+
+def _fma(a, b, c):
+    return _rn32(a * b + c)
+
+
+def _two_sum(a, b):
+    s = _add(a, b)
+    bb = _add(s, -a)
+    return s, _add(_add(a, -_add(s, -bb)), _add(b, -bb))
+
+
+def _fast_two_sum(a, b):
+    s = _add(a, b)
+    return s, _add(b, -_add(s, -a))
+
+
+def _cmul_add(ar, ai, br, bi, c, d):
+    """ff32.cuh's ff_cmul_add, step for step, on (hi, lo) pairs of Fractions."""
+    p1 = _mul(ar[0], br[0]); e1 = _fma(ar[0], br[0], -p1)
+    p2 = _mul(ai[0], bi[0]); e2 = _fma(ai[0], bi[0], -p2)
+    s = _two_sum(p1, -p2)
+    s2 = _two_sum(s[0], c[0])
+    lo = _add(_add(s[1], s2[1]), _add(e1, -e2))
+    lo = _fma(ar[0], br[1], lo)
+    lo = _fma(ar[1], br[0], lo)
+    lo = _fma(-ai[0], bi[1], lo)
+    lo = _fma(-ai[1], bi[0], lo)
+    lo = _add(lo, c[1])
+    outr = _fast_two_sum(s2[0], lo)
+    p1 = _mul(ar[0], bi[0]); e1 = _fma(ar[0], bi[0], -p1)
+    p2 = _mul(ai[0], br[0]); e2 = _fma(ai[0], br[0], -p2)
+    s = _two_sum(p1, p2)
+    s2 = _two_sum(s[0], d[0])
+    lo = _add(_add(s[1], s2[1]), _add(e1, e2))
+    lo = _fma(ar[0], bi[1], lo)
+    lo = _fma(ar[1], bi[0], lo)
+    lo = _fma(ai[0], br[1], lo)
+    lo = _fma(ai[1], br[0], lo)
+    lo = _add(lo, d[1])
+    outi = _fast_two_sum(s2[0], lo)
+    return outr, outi
+
+
+def _ffq(x):
+    h = _rn32(Q(x))
+    return h, _rn32(Q(x) - h)
+
+
+def test_float_float_multiply_add_rounding_bound():
+    """|delta' - (t delta + eps)| <= u (|t.h|_1 |delta.h|_1 + |eps|_1), u = 0x1.2p-43
+    (the FE32 certificate's kFeU; its derivation takes every low-word term at
+    its worst)."""
+    rng = np.random.default_rng(13)
+    u = Q(9, 8) * Q(1, 2 ** 43)
+    worst = Q(0)
+    for _ in range(4000):
+        t = [_ffq(rng.uniform(-4, 4) * 10.0 ** rng.integers(-2, 1)) for _ in range(2)]
+        dl = [_ffq(rng.uniform(-1, 1) * 10.0 ** rng.integers(-8, 0)) for _ in range(2)]
+        ep = [_ffq(rng.uniform(-1, 1) * 10.0 ** rng.integers(-10, -2)) for _ in range(2)]
+        (nr, ni) = _cmul_add(t[0], t[1], dl[0], dl[1], ep[0], ep[1])
+        T = [a[0] + a[1] for a in t]
+        D = [a[0] + a[1] for a in dl]
+        E = [a[0] + a[1] for a in ep]
+        xr = T[0] * D[0] - T[1] * D[1] + E[0]
+        xi = T[0] * D[1] + T[1] * D[0] + E[1]
+        err = abs(nr[0] + nr[1] - xr) + abs(ni[0] + ni[1] - xi)
+        bound = u * ((abs(t[0][0]) + abs(t[1][0])) * (abs(dl[0][0]) + abs(dl[1][0]))
+                     + abs(ep[0][0]) + abs(ep[1][0]))
+        assert err <= bound
+        worst = max(worst, err / bound)
+    assert worst > Q(1, 1000)  # not vacuous

@@ -4,18 +4,23 @@
 // Two arrangements of the same arithmetic:
 //
 // * The pass pipeline (the FE32 path of nm_render_rows):
-//     fe_front_kernel  one thread per sample, FP64: the series front of
-//                      getIterations (pixel_fp64.cuh, bit-identical to the
-//                      plain FP64 path); writes the sample's start state and
-//                      appends it to a work list, or finishes it (cardioid,
-//                      escape before the skip point).
-//     fe_iter_kernel   persistent and warp-refilled over the work list, FP32
-//                      only: the delta iteration and the smoothing term,
-//                      written to the grid; appends every sample it could not
-//                      certify to the rework list.
-//   followed by the plain FP64 kernel over the rework list.  FP64 runs only
-//   in converged warps: GB300 issues FP64 at 1/64 of the FP32 rate, and FP64
-//   inside a refill loop costs a warp's full instruction stream per lane.
+//     fe_front_kernel   one thread per sample: the series front of
+//                       getIterations -- its stop index searched in FP32 with
+//                       a guard band, the FP64 front (pixel_fp64.cuh,
+//                       bit-identical to the plain FP64 path) only where that
+//                       search cannot decide; writes the sample's start state
+//                       and appends it to a work list, or finishes it
+//                       (cardioid, escape before the skip point).
+//     fe_overlap_kernel persistent and warp-refilled over the work list: six
+//                       warps a block run the FP32 delta iteration and the
+//                       smoothing term, appending every sample they cannot
+//                       certify to the rework list, which the other two warps
+//                       render in FP64 meanwhile (fe_iter_kernel: the FP32
+//                       warps alone, the rework after the pass).
+//   followed by the plain FP64 kernel over what is left of the rework list.
+//   FP64 runs only in converged warps: GB300 issues FP64 at about 1/75 of the
+//   FP32 rate, and a warp instruction costs the FP64 pipe the same whatever
+//   its active lanes.
 //
 // * The single-pass kernel fe32_kernel: front, iteration and smoothing in one
 //   persistent kernel (the FP64 front inside the refill loop).  Its scratch is only the

@@ -2,7 +2,8 @@
 // iteration count) in one sequence of launches that the host captures into a
 // single CUDA graph.  Frames are grouped by the kernel that renders them:
 //
-//   FE32 frames:  batch_front_kernel (FP64 series front, converged),
+//   FE32 frames:  batch_front_kernel (series front: FP32 stop-index search,
+//                                     the FP64 front where it cannot decide),
 //                 batch_overlap_kernel (FP32 iteration and smoothing,
 //                                     persistent over all FE32 frames'
 //                                     samples at once, with the double-path

@@ -311,7 +311,12 @@ __device__ __forceinline__ void persistent_loop(const DeviceView& v, const Rende
 // entry still unwritten after kEntryPolls polls is counted in `timeouts` and
 // skipped and left unrendered (the host sees the count).
 
-constexpr unsigned kDrainIdlePolls = 1u << 19;  // about a second of 2 us sleeps
+// An idle consumer sleeps 20 us between polls, 2^16 polls: about a second.
+// (With 2 us sleeps the 1920x1080x16 view at width 1e-12 took 186 ms instead
+// of 183 -- the FE32 warps beside the pollers lose issue slots; 100 us was
+// slower again.)
+constexpr unsigned kDrainNapNs = 20000;
+constexpr unsigned kDrainIdlePolls = 1u << 16;
 constexpr unsigned kEntryPolls = 1u << 16;
 
 enum ClaimStatus { CLAIM_OK = 0, CLAIM_EMPTY = 1, CLAIM_BUSY = 2 };
@@ -425,7 +430,7 @@ __device__ __forceinline__ void drain_loop(const Src& src, const RenderCtl& ctl,
     if (!__any_sync(kFull, active)) {
       if (!pool ? fin : idle > 2 * kDrainIdlePolls) break;
       ++idle;
-      __nanosleep(2000);
+      __nanosleep(kDrainNapNs);
       continue;
     }
     idle = 0;

@@ -170,3 +170,16 @@ def test_float_float_multiply_add_rounding_bound():
         assert err <= bound
         worst = max(worst, err / bound)
     assert worst > Q(1, 1000)  # not vacuous
+
+
+def test_eps_below_the_double_range_is_below_half_an_ulp():
+    """The plain FP64 step on floatexp views leaves out an eps component below
+    2^-1022 (pixel_xd.cuh: plain_eps): exact because every sum it would be
+    added to is nonzero and at least 2^-400 in magnitude (the guard), so the
+    correctly rounded sum is the sum itself."""
+    rng = np.random.default_rng(14)
+    for _ in range(20000):
+        q = float(rng.uniform(1.0, 2.0) * 2.0 ** int(rng.integers(-400, 60)) * rng.choice([-1, 1]))
+        eps = Q(int(rng.integers(1, 2 ** 53)), 2 ** int(rng.integers(1075, 1700)))  # < 2^-1022
+        eps = eps if rng.random() < 0.5 else -eps
+        assert float(Q(q) + eps) == q  # float(Fraction) rounds to nearest

@@ -183,3 +183,22 @@ def test_eps_below_the_double_range_is_below_half_an_ulp():
         eps = Q(int(rng.integers(1, 2 ** 53)), 2 ** int(rng.integers(1075, 1700)))  # < 2^-1022
         eps = eps if rng.random() < 0.5 else -eps
         assert float(Q(q) + eps) == q  # float(Fraction) rounds to nearest
+
+
+def test_quick_bailout_decision_is_implied():
+    """fe_core.cuh decides the bailout test without evaluating it while
+    |Y|^2 <= 2^20 (1 - 2^-10), Z is not the orbit's escaped last point and the
+    bound e < 0.2: then |Z.h|_1 < 1449 and |delta.h|_1 < 2900, and the full test's
+    band 2 (2^-20 (|Z| + |delta|) + yerr) stays below 1024 - |Y|.  Checked at the
+    extremes of those ranges, in exact arithmetic."""
+    kfeu, kfeuz = Q(9, 8) * Q(1, 2 ** 43), Q(1, 2 ** 45)
+    lo_band = Q(2 ** 20) * (1 - Q(1, 2 ** 10))
+    ym_max = Q(1024) * (1 - Q(1, 2 ** 11)) * (1 + Q(1, 2 ** 21))  # sqrt(lo_band) and rsqrt's error
+    assert ym_max ** 2 >= lo_band
+    zn1, dn1, err = Q(1449), Q(2900), Q(1, 5)
+    yerr = err + kfeuz * zn1 + kfeu * (zn1 + dn1)
+    band = 2 * (Q(1, 2 ** 20) * (zn1 + dn1) + yerr)
+    assert band < 1024 - ym_max
+    # and the ranges themselves: a non-escaped orbit point and |Y| <= 1024
+    assert Q(1448) ** 2 < 2 * Q(2 ** 20) < Q(1449) ** 2  # |Z|_1 <= sqrt(2) * 1024
+    assert 2 * Q(1449) < 2900

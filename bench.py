@@ -10,8 +10,14 @@ samples counted as N) over the render time.
 
 `value`  : device time of the render kernel, inputs resident, L2 flushed
            between steps.
-`e2e`    : the same through the C ABI with host buffers: upload of the step's
-           tables, render, multisample reduce, copy of the reduced grid to host.
+`e2e`    : the same through the C ABI with host buffers, as the reference
+           renders a view: the host precompute (probe search, orbit, series),
+           upload of its tables, render, multisample reduce, copy of the
+           reduced grid to host.
+The line also carries `c3_deep`: the 3840x2160 view at width 1e-300 rendered
+on the FE32 path and, for comparison, on the plain FP64 path over the whole
+frame; and `exact_vs_reference_mp`: both C2 grids against the reference's own
+arbitrary-precision continuation on a seeded sample.
 --impl reference : the reference algorithm (the oracle's restatement of
            mandelbrot.cpp, arbitrary-precision continuation) on the host cores.
 
@@ -214,6 +220,111 @@ def cpu_reference(seconds, threads, seed=7):
     return total_it / elapsed, total_px, threads
 
 
+def reference_agreement(nm, m, fp, n_samples, seed=11):
+    """Escape counts of the FE32 grid (m) and the FP64 grid (fp) against the
+    reference's own semantics -- getIterations with its arbitrary-precision
+    continuation (the oracle's MODE_REF) -- on a seeded random sample of the
+    workload's samples, on all host threads."""
+    from oracle import oracle
+    threads = os.cpu_count() or 1
+    o = oracle.OracleView(NR, NC)
+    o.set_view(CENTER[0], CENTER[1], step_string(), step_string(), N_ITER, TOL)
+    o.scale_up(SC)
+    o.precompute(threads=threads)
+    nr, nc = o.rows, o.cols
+    rng = np.random.default_rng(seed)
+    k = rng.choice(nr * nc, size=n_samples, replace=False)
+    rr, cc = (k // nc).astype(np.int32), (k % nc).astype(np.int32)
+    t0 = time.perf_counter()
+    it, _ = o.render_pixels(rr, cc, oracle.MODE_REF, threads=threads)
+    cpu_s = time.perf_counter() - t0
+    out = {"samples": int(n_samples), "seed": seed, "oracle": "MODE_REF (MP continuation)",
+           "cpu_s": cpu_s, "threads": threads}
+    for name, g in (("fe32", m), ("fp64", fp)):
+        gi = g[rr, cc]
+        out["exact_" + name] = float((gi == it).mean())
+    return out
+
+
+def c3_deep(nm, steps, flush, stream):
+    """The 3840x2160 view at width 1e-300 (N 1,000,000, 1100-bit orbit at the
+    view center, floatexp series; seeded boundary-following center): the FE32
+    frame timed over `steps` renders, and the plain FP64 path over the WHOLE
+    frame on the same orbit, with the exact-count fraction between them."""
+    from decimal import Decimal, getcontext
+    nr, nc, N, bits = 2160, 3840, 1000000, 1100
+    cre, cim, width = deep_view()
+    getcontext().prec = 340
+    step = str(Decimal(width) / nc)
+    m = nm.Mandelbrot(nr, nc)
+    m.set_view(cre, cim, step, step, N, TOL, bits)
+    m.set_path(nm.PATH_FE32)
+    m.set_option(nm.OPT_REFERENCE, nm.REFERENCE_CENTER)
+    m.set_option(nm.OPT_KEEP_SMOOTH64, 1)
+    t0 = time.perf_counter()
+    m.precompute()
+    precompute_s = time.perf_counter() - t0
+    m.upload()
+
+    def timed(mm, k, w):
+        ts = []
+        for i in range(w + k):
+            with torch_stream(stream):
+                flush.zero_()
+            e0, e1 = cuda_events()
+            e0.record(stream)
+            mm.render_rows(0, mm.rows(), stream.cuda_stream)
+            e1.record(stream)
+            mm.synchronize()
+            stream.synchronize()
+            if i >= w:
+                ts.append(e0.elapsed_time(e1))
+        return ts
+
+    fe_times = timed(m, steps, 1)
+    fe_ms = float(np.mean(fe_times))
+    g = m.grid()
+    s64 = m.smoothing64()
+    eff = int(g["iterations"].astype(np.int64).sum())
+    executed = m.stat(nm.STAT_EXECUTED_ITERS)
+    rework = m.stat(nm.STAT_FP64_REWORK)
+    timeouts = m.stat(nm.STAT_WAIT_TIMEOUTS)
+    fp = m.copy()
+    fp.set_path(nm.PATH_FP64)
+    fp.set_option(nm.OPT_KEEP_SMOOTH64, 1)
+    fp.upload()
+    fp_times = timed(fp, 1, 0)
+    fp_ms = float(np.mean(fp_times))
+    gf = fp.grid()
+    same = gf["iterations"] == g["iterations"]
+    d = np.abs(fp.smoothing64() - s64)[same]
+    fe_rate = eff / (fe_ms * 1e-3)
+    fp_rate = eff / (fp_ms * 1e-3)
+    return {"workload": "3840x2160, 1 sample a pixel, width 1e-300, N 1000000, 1100-bit "
+                        "orbit at the seeded deep center, floatexp series",
+            "width": width, "orbit_length": m.stat(nm.STAT_ORBIT_LENGTH),
+            "precompute_s": precompute_s, "fe32_ms": fe_ms,
+            "fe32_step_ms": [round(t, 3) for t in fe_times], "fe32_value": fe_rate,
+            "fp64_ms_whole_frame": fp_ms, "fp64_value": fp_rate, "unit": "pixel-iters/s",
+            "speedup_vs_fp64": fp_ms / fe_ms,
+            "exact_iter_fraction_vs_fp64": float(same.mean()),
+            "max_dsmooth_exact_samples": float(d.max()) if d.size else None,
+            "executed_iters": executed, "effective_iters": eff,
+            "executed_iters_per_s": executed / (fe_ms * 1e-3),
+            "fp64_rework_samples": rework, "wait_timeouts": timeouts,
+            "interior_fraction": float((g["iterations"] == N).mean())}
+
+
+def torch_stream(stream):
+    import torch
+    return torch.cuda.stream(stream)
+
+
+def cuda_events():
+    import torch
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
 def run_reference(args):
     world, rank, _ = dist_setup()
     if rank != 0:
@@ -294,6 +405,7 @@ def run_ours(args):
                 e0.record(stream)
                 mm.render_rows(0, mm.rows(), stream.cuda_stream)
                 e1.record(stream)
+            mm.synchronize()
             stream.synchronize()
             if i >= w:
                 times.append(e0.elapsed_time(e1))
@@ -303,10 +415,12 @@ def run_ours(args):
     barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
+        launches0 = m.stat(nm.STAT_KERNEL_LAUNCHES)
         wall0 = time.perf_counter()
         times = render_timed(m, args.steps, 0)
         torch.cuda.synchronize()
         wall = time.perf_counter() - wall0
+        launches = m.stat(nm.STAT_KERNEL_LAUNCHES) - launches0
     barrier()
     ms = max_over_ranks(float(np.mean(times)), device="cuda")
     g = m.grid()
@@ -314,6 +428,7 @@ def run_ours(args):
     executed = m.stat(nm.STAT_EXECUTED_ITERS)
     rework = m.stat(nm.STAT_FP64_REWORK)
     front_fp64 = m.stat(nm.STAT_FRONT_FP64)
+    timeouts = m.stat(nm.STAT_WAIT_TIMEOUTS)
     k_main_ms = m.stat(nm.STAT_KERNEL_NS) * 1e-6
     k_rework_ms = m.stat(nm.STAT_REWORK_KERNEL_NS) * 1e-6
     k_iter_ms = m.stat(nm.STAT_ITER_KERNEL_NS) * 1e-6
@@ -332,18 +447,29 @@ def run_ours(args):
     red_fe = m.reduce(SC)
     red_fp = fp.reduce(SC)
     exact_px = float((red_fe["iterations"] == red_fp["iterations"]).mean())
+    agreement = None
+    if rank == 0 and not args.no_cpu and args.ref_samples > 0:
+        agreement = reference_agreement(nm, g["iterations"], gf["iterations"], args.ref_samples)
     del gf, dsm, same
 
-    # e2e through the C ABI with host buffers
+    # e2e through the C ABI with host buffers, as the reference renders a view
+    # (precompute(), then the rows): the host precompute (probe search, orbit,
+    # series), the upload of its tables, the render, the multisample reduce and
+    # the copy of the reduced grid to host; L2 flushed before every step
     red = np.empty((NR, NC), nm.ESCAPE_DTYPE)
-    e2e_times = []
+    e2e_times, pre_times = [], []
     for i in range(1 + args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
         t0 = time.perf_counter()
+        m.precompute()
+        t1 = time.perf_counter()
         m.upload()
         m.render()
         m.reduce(SC, red)
         if i:
             e2e_times.append(time.perf_counter() - t0)
+            pre_times.append(t1 - t0)
     e2e_s = float(np.mean(e2e_times))
     n_sample = NR * SC * NC * SC
     h2d = 16 * (NC * SC + NR * SC) + 8 * (NC * SC + NR * SC)
@@ -376,9 +502,11 @@ def run_ours(args):
             "kernel_ms": {"render_passes": k_main_ms, "iteration_pass": k_iter_ms,
                           "fp64_rework": k_rework_ms},
             "executed_iters_per_step": executed, "effective_iters_per_step": eff_iters,
+            "executed_iters_per_s": executed / (ms * 1e-3),
+            "wait_timeouts": timeouts,
             "precompute_s": precompute_s, "wall_s": wall,
-            # FE32: front, iteration, smoothing and FP64 rework kernels per step
-            "gpu_launches": (4 if primary == nm.PATH_FE32 else 1) * args.steps,
+            # kernels the library launched during the timed steps (its own count)
+            "gpu_launches": launches,
             "roofline": {"bound": "fp32" if primary == nm.PATH_FE32 else "fp64",
                          "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
                          "frac": achieved / peak, "traffic": None,
@@ -393,7 +521,12 @@ def run_ours(args):
                              executed, k_iter_ms, clocks.summary())},
             "clocks": clocks.summary(),
             "e2e": {"value": eff_iters / e2e_s, "unit": "pixel-iters/s",
-                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": NR * NC * 8},
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": NR * NC * 8,
+                    "ms_per_step": e2e_s * 1e3,
+                    "precompute_ms": float(np.mean(pre_times)) * 1e3,
+                    "includes": "nm_precompute (host probe search, orbit, series), table "
+                                "upload, render, reduce, reduced grid to host; L2 flushed"},
+            "exact_vs_reference_mp": agreement,
         }
         if not args.no_cpu:
             v, px, cores = cpu_reference(args.cpu_seconds, 1)
@@ -402,6 +535,8 @@ def run_ours(args):
                                     "sample": "%d random samples of the 33,177,600, reference "
                                               "getIterations (MP continuation), 1 thread" % px}
             line["c1_double_loop"] = c1_double_loop(nm)
+        if not args.no_deep:
+            line["c3_deep"] = c3_deep(nm, max(1, min(args.steps, 5)), flush, stream)
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -775,6 +910,10 @@ def main():
     ap.add_argument("--path", default="fe32", choices=["fe32", "fp64"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-deep", action="store_true",
+                    help="leave out the 3840x2160 width-1e-300 comparison of the default line")
+    ap.add_argument("--ref-samples", type=int, default=100000,
+                    help="samples of the reference-semantics (MP continuation) check")
     ap.add_argument("--profile", type=int, default=0,
                     help="render each path once on a 1/DIV-size crop and exit (ncu case)")
     ap.add_argument("--workload", default="c2", choices=["c2", "video", "deep", "learned"])

@@ -88,7 +88,9 @@ enum nm_stat {
   NM_STAT_PRECOMPUTE_US = 19,     /* host time of the last nm_precompute */
   NM_STAT_KERNEL_NS = 20,         /* GPU time of the last render's main kernel */
   NM_STAT_REWORK_KERNEL_NS = 21,  /* GPU time of the last FE32 render's FP64 rework */
-  NM_STAT_ITER_KERNEL_NS = 22     /* GPU time of the last FE32 render's iteration pass */
+  NM_STAT_ITER_KERNEL_NS = 22,    /* GPU time of the last FE32 render's iteration pass */
+  NM_STAT_KERNEL_LAUNCHES = 23    /* kernels this library launched in this process, over all
+                                     handles (a batch's graph replay adds its kernels) */
 };
 
 /* Mandelbrot::Mandelbrot(int nr, int nc), mandelbrot.cpp:8-17: center -0.5,
@@ -275,9 +277,15 @@ int nm_batch_autotune(nm_batch* b, int stride, int* tile_w, int* tile_h, int* re
    held by every GPU that loads the library until the process exits; views
    of more than NM_NOALLOC_MAX_SAMPLES samples are refused with NM_ERR_ARG.
    The first call on a device looks the array up (cudaGetSymbolAddress):
-   make that first call before any stream capture.  All calls share the one
+   make that first call before any stream capture.  The handle's device must
+   be the current device (else NM_ERR_STATE).  All calls share the one
    array, so calls whose kernels overlap on the GPU (other streams or
-   threads) race: serialise them. */
+   threads) race: serialise them.  The escape counts are those of nm_render
+   on the FE32 path; on views where the reference takes its double loop the
+   interior-orbit trapping is off here (it needs a per-sample record), so
+   such views render the same counts more slowly.  The call's statistics
+   (executed steps, reworked samples) stay in the scratch array: nm_get_stat
+   reports the handle's own renders only. */
 #define NM_NOALLOC_MAX_SAMPLES 4194304
 int nm_render_fe32_noalloc(nm_handle* h, nm_escape_value* out, void* stream);
 

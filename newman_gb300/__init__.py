@@ -26,7 +26,7 @@ REFERENCE_PROBES, REFERENCE_CENTER = 0, 1
 STAT_CARDIOID_UNDECIDED, STAT_EXECUTED_ITERS, STAT_SAMPLES, STAT_REBASES, STAT_FP64_REWORK, \
     STAT_WAIT_TIMEOUTS, STAT_FRONT_FP64 = range(7)
 STAT_ORBIT_LENGTH, STAT_PROBE_INDEX, STAT_PRECISION_BITS, STAT_PRECOMPUTE_US = 16, 17, 18, 19
-STAT_KERNEL_NS, STAT_REWORK_KERNEL_NS, STAT_ITER_KERNEL_NS = 20, 21, 22
+STAT_KERNEL_NS, STAT_REWORK_KERNEL_NS, STAT_ITER_KERNEL_NS, STAT_KERNEL_LAUNCHES = 20, 21, 22, 23
 
 COST_FEATURES, COST_PARAMS = 18, 9601
 

@@ -27,8 +27,11 @@ struct nm_batch {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool built = false;
   cudaGraphExec_t exec = nullptr;
+  long long graph_kernels = 0;  // kernel launches captured in exec
   nmg::BatchLaunch L{};
-  // what the graph was built against, to notice changed frames
+  // what the graph was built against, to notice changed frames: each frame's
+  // generation (nm_handle::generation) and buffers
+  std::vector<unsigned long long> seen_gen;
   std::vector<const void*> seen_grid, seen_orbit;
 
   DevBuf<nmg::DeviceView> d_views_fe, d_views_hw, d_views_fp64;
@@ -104,6 +107,7 @@ int build(nm_batch* b) {
   std::vector<long long> off_fe{0}, off_hw{0}, off_fp64{0};
   std::vector<nmg::ReduceJob> red;
   long long red_total = 0;
+  b->seen_gen.clear();
   b->seen_grid.clear();
   b->seen_orbit.clear();
   for (nm_handle* h : b->frames) {
@@ -132,6 +136,7 @@ int build(nm_batch* b) {
       red.push_back(j);
       red_total += (long long)(h->view.rows() / b->sc) * j.nc;
     }
+    b->seen_gen.push_back(h->generation);
     b->seen_grid.push_back(h->grid.p);
     b->seen_orbit.push_back(h->d_zf.p);
   }
@@ -189,10 +194,14 @@ int build(nm_batch* b) {
 
   if (b->use_graph) {
     cudaGraph_t graph = nullptr;
+    const long long launches0 = nmg::launches_so_far();
     NM_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     cudaError_t e = cudaMemsetAsync(b->d_scratch.p, 0, kBatchWords * 8, s);
     if (e == cudaSuccess) e = nmg::launch_batch(L, s);
     cudaError_t e2 = cudaStreamEndCapture(s, &graph);
+    // captured, not run: a replay counts them
+    b->graph_kernels = nmg::launches_so_far() - launches0;
+    nmg::note_launches(-b->graph_kernels);
     if (e != cudaSuccess || e2 != cudaSuccess) {
       if (graph) cudaGraphDestroy(graph);
       return fail(NM_ERR_CUDA, "batch graph capture: %s",
@@ -210,7 +219,8 @@ bool stale(const nm_batch* b) {
   if (!b->built || b->seen_grid.size() != b->frames.size()) return true;
   for (size_t k = 0; k < b->frames.size(); k++) {
     const nm_handle* h = b->frames[k];
-    if (!h->uploaded || h->grid.p != b->seen_grid[k] || h->d_zf.p != b->seen_orbit[k])
+    if (!h->uploaded || h->generation != b->seen_gen[k] || h->grid.p != b->seen_grid[k] ||
+        h->d_zf.p != b->seen_orbit[k])
       return true;
   }
   return false;
@@ -293,18 +303,38 @@ int nm_batch_render(nm_batch* b) {
   NM_CUDA(cudaEventRecord(b->ev0, b->stream));
   if (b->use_graph) {
     NM_CUDA(cudaGraphLaunch(b->exec, b->stream));
+    nmg::note_launches(b->graph_kernels);
   } else {
     NM_CUDA(cudaMemsetAsync(b->d_scratch.p, 0, kBatchWords * 8, b->stream));
     NM_CUDA(nmg::launch_batch(b->L, b->stream));
   }
   NM_CUDA(cudaEventRecord(b->ev1, b->stream));
   NM_CUDA(cudaStreamSynchronize(b->stream));
+  if (b->overlap && b->L.fe.n > 0 && b->L.fe.total > 0) {
+    // An overlapped FP64 consumer skips a rework entry it claimed but could not
+    // read within its poll limit (counted as a wait timeout).  Every entry is
+    // written once the launches have ended: render the whole rework list again
+    // in FP64 (the same results for the samples already rendered) and reduce
+    // the frames again.
+    unsigned long long lost = 0;
+    NM_CUDA(cudaMemcpy(&lost, b->d_scratch.p + kFeStats + nmg::STAT_WAIT_TIMEOUTS, 8,
+                       cudaMemcpyDeviceToHost));
+    if (lost) {
+      NM_CUDA(cudaMemsetAsync(b->d_scratch.p + kReworkNext, 0, 8, b->stream));
+      NM_CUDA(nmg::launch_batch_rework(b->L, b->stream));
+      NM_CUDA(cudaStreamSynchronize(b->stream));
+    }
+  }
   return NM_OK;
 }
 
 int nm_batch_get_stat(nm_batch* b, int stat, long long* value) {
   if (!b || !value) return fail(NM_ERR_ARG, "null batch or output");
   *value = 0;
+  if (stat == NM_STAT_KERNEL_LAUNCHES) {
+    *value = nmg::launches_so_far();
+    return NM_OK;
+  }
   if (!b->built) return NM_OK;
   if (stat == NM_STAT_KERNEL_NS) {
     float ms = 0.f;

@@ -103,6 +103,7 @@ int ensure_grid(nm_handle* h) {
   }
   h->grid_nr = nr;
   h->grid_nc = nc;
+  h->generation++;
   return NM_OK;
 }
 
@@ -175,6 +176,7 @@ int do_upload(nm_handle* h) {
   // reaches this point, so wait before the host may touch them again.
   NM_CUDA(cudaStreamSynchronize(h->stream));
   h->uploaded = true;
+  h->generation++;
   return NM_OK;
 }
 
@@ -442,6 +444,7 @@ int nm_set_iterations(nm_handle* h, int N) {
   h->view.set_iterations(N);
   h->precomputed = false;
   h->uploaded = false;
+  h->generation++;
   return NM_OK;
 }
 int nm_get_iterations(const nm_handle* h) { return h ? h->view.iterations() : -1; }
@@ -451,6 +454,7 @@ int nm_set_tolerance(nm_handle* h, double tol) {
   h->view.set_tolerance(tol);
   h->precomputed = false;
   h->uploaded = false;
+  h->generation++;
   return NM_OK;
 }
 int nm_rows(const nm_handle* h) { return h ? h->view.rows() : -1; }
@@ -461,11 +465,13 @@ int nm_set_path(nm_handle* h, int path) {
   if (int rc = check_handle(h)) return rc;
   if (path < NM_PATH_REFERENCE || path > NM_PATH_FE32) return fail(NM_ERR_ARG, "bad path %d", path);
   h->path = path;
+  h->generation++;
   return NM_OK;
 }
 
 int nm_set_option(nm_handle* h, int opt, long long value) {
   if (int rc = check_handle(h)) return rc;
+  h->generation++;
   switch (opt) {
     case NM_OPT_TILE_W:
     case NM_OPT_TILE_H:
@@ -531,6 +537,7 @@ int nm_get_stat(nm_handle* h, int stat, long long* value) {
     case NM_STAT_PROBE_INDEX: *value = h->precomputed ? h->od.probe_index : -1; return NM_OK;
     case NM_STAT_PRECISION_BITS: *value = (long long)h->view.bits(); return NM_OK;
     case NM_STAT_PRECOMPUTE_US: *value = (long long)h->precompute_us; return NM_OK;
+    case NM_STAT_KERNEL_LAUNCHES: *value = nmg::launches_so_far(); return NM_OK;
     case NM_STAT_KERNEL_NS:
     case NM_STAT_REWORK_KERNEL_NS:
     case NM_STAT_ITER_KERNEL_NS: {
@@ -581,6 +588,7 @@ int nm_precompute(nm_handle* h) {
   h->precompute_us =
       std::chrono::duration<double, std::micro>(std::chrono::steady_clock::now() - t0).count();
   h->uploaded = false;  // copied to the GPU by nm_upload or the next render
+  h->generation++;
   return NM_OK;
 }
 
@@ -613,6 +621,8 @@ int nm_render_rows(nm_handle* h, int r0, int r1, void* stream_arg) {
   nmg::KernelKind kind;
   if (int rc = prepare_view(h, r0, r1, v, kind)) return rc;
   cudaStream_t s = stream_arg ? (cudaStream_t)stream_arg : h->stream;
+  h->render_stream = s;
+  h->last_overlapped = false;
   nmg::RenderCtl ctl;
   std::memset(&ctl, 0, sizeof ctl);
   ctl.next = h->d_scratch.p + kNextMain;
@@ -667,6 +677,8 @@ int nm_render_rows(nm_handle* h, int r0, int r1, void* stream_arg) {
     NM_CUDA(nmg::launch_fe32_passes(v, b, ctl, s, h->device, h->blocks, chunk, h->ev[3],
                                     h->ev[4], h->fe_overlap ? &o : nullptr));
     h->timed_iter = true;
+    h->last_overlapped = h->fe_overlap;
+    h->last_view = v;
   } else {
     NM_CUDA(nmg::launch_render(kind, v, ctl, s, blocks, chunk));
   }
@@ -687,7 +699,28 @@ int nm_render_rows(nm_handle* h, int r0, int r1, void* stream_arg) {
 int nm_synchronize(nm_handle* h) {
   if (int rc = check_handle(h)) return rc;
   if (!h->stream) return NM_OK;
-  NM_CUDA(cudaStreamSynchronize(h->stream));
+  cudaStream_t s = h->render_stream ? h->render_stream : h->stream;
+  NM_CUDA(cudaStreamSynchronize(s));
+  if (s != h->stream) NM_CUDA(cudaStreamSynchronize(h->stream));
+  if (h->last_overlapped) {
+    // An overlapped FP64 consumer skips a rework entry it claimed but could not
+    // read within its poll limit (counted in STAT_WAIT_TIMEOUTS).  Every entry
+    // is written once the launch has ended, so the whole list is rendered
+    // again in FP64 -- the same results for the samples already rendered.
+    h->last_overlapped = false;
+    unsigned long long lost = 0;
+    NM_CUDA(cudaMemcpy(&lost, h->d_scratch.p + kStatsMain + nmg::STAT_WAIT_TIMEOUTS, 8,
+                       cudaMemcpyDeviceToHost));
+    if (lost && !*h->cancel_host) {
+      nmg::RenderCtl main{};
+      main.cancel = h->cancel_dev;
+      const nmg::RenderCtl re = rework_ctl(h, main);
+      NM_CUDA(cudaMemsetAsync(h->d_scratch.p + kNextRework, 0, 8, s));
+      NM_CUDA(nmg::launch_render(nmg::KERNEL_REWORK, h->last_view, re, s,
+                                 nmg::persistent_blocks(nmg::KERNEL_REWORK, h->device), h->chunk));
+      NM_CUDA(cudaStreamSynchronize(s));
+    }
+  }
   if (*h->cancel_host) {
     unsigned long long done = 0;
     NM_CUDA(cudaMemcpy(&done, h->d_scratch.p + kStatsMain + nmg::STAT_SAMPLES, 8,
@@ -721,6 +754,7 @@ int nm_set_tile_order(nm_handle* h, const int* order, int n) {
   if (int rc = check_handle(h)) return rc;
   if (!order || n == 0) {
     h->tile_order.clear();
+    h->generation++;
     return NM_OK;
   }
   int tx = 0, ty = 0;
@@ -733,6 +767,7 @@ int nm_set_tile_order(nm_handle* h, const int* order, int n) {
       return fail(NM_ERR_ARG, "tile order is not a permutation (entry %d = %d)", k, order[k]);
     seen[(size_t)order[k]] = 1;
   }
+  h->generation++;
   h->tile_order.assign(order, order + n);
   h->tile_order_w = h->tile_w;
   h->tile_order_h = h->tile_h;

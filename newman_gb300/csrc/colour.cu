@@ -6,6 +6,8 @@
 // host's byte for byte.
 #include <cuda_runtime.h>
 
+#include "engine.hpp"
+
 #include <cstdint>
 
 #include "colour.hpp"
@@ -85,6 +87,7 @@ cudaError_t launch_colour(const EscapeValue* grid, int nr, int nc, int sc, int N
   if (n <= 0) return cudaSuccess;
   long long blocks = (n + 255) / 256;
   if (blocks > 152 * 32) blocks = 152 * 32;
+  nmg::note_launches(1);
   colour_kernel<<<(int)blocks, 256, 0, s>>>(grid, nr, nc, sc, N, pal, smooth, out);
   return cudaGetLastError();
 }

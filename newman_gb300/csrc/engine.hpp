@@ -104,6 +104,14 @@ struct BatchLaunch {
 };
 // Every launch of one batch render, in stream order (capturable).
 cudaError_t launch_batch(const BatchLaunch& launch, cudaStream_t stream);
+// The FP64 render of the batch's rework list from its claim counter on (the
+// caller resets it), then the multisample reduce of every frame.
+cudaError_t launch_batch_rework(const BatchLaunch& launch, cudaStream_t stream);
+
+// Kernels launched by this library in this process (all handles; a graph
+// replay counts its kernel nodes).  note_launches adds n.
+void note_launches(long long n);
+long long launches_so_far();
 
 // Persistent, warp-refilled launches: every warp keeps its 32 lanes busy by
 // pulling new samples from `ctl.next` as lanes finish.

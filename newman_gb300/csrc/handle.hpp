@@ -138,6 +138,20 @@ struct nm_handle {
   DevBuf<unsigned long long> d_tile_cost;
   long long cost_tiles = 0;
 
+  // Bumped by every change that can alter what a render of this handle
+  // launches (view, N, tolerance, path, options, tables, their upload, the
+  // grid): a batch records it per frame when it captures its graph and
+  // rebuilds the graph when it differs.
+  unsigned long long generation = 0;
+  // The stream of the last nm_render_rows (the handle's own or the caller's),
+  // which nm_synchronize waits for.
+  cudaStream_t render_stream = nullptr;
+  // The last render's device view, when it was an FE32 render with the FP64
+  // rework overlapped: nm_synchronize re-renders its rework list if any of the
+  // overlapped pass's bounded waits ran out.
+  bool last_overlapped = false;
+  nmg::DeviceView last_view{};
+
   nm_handle(int nr, int nc) : view(nr, nc) {}
   ~nm_handle() {
     for (cudaEvent_t e : ev)
@@ -149,6 +163,7 @@ struct nm_handle {
     precomputed = false;
     coords_valid = false;
     uploaded = false;
+    generation++;
   }
 };
 

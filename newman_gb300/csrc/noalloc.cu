@@ -81,6 +81,15 @@ extern "C" int nm_render_fe32_noalloc(nm_handle* h, nm_escape_value* out, void* 
     nmg::noalloc_fail("nm_render_fe32_noalloc: " + why);
     return rc;
   }
+  // The handle's tables, the scratch address looked up below and the kernels
+  // all belong to the handle's device, which must be the current one.
+  int current = -1;
+  if (cudaGetDevice(&current) != cudaSuccess || current != device) {
+    nmg::noalloc_fail("nm_render_fe32_noalloc: the handle belongs to device " +
+                      std::to_string(device) + " but device " + std::to_string(current) +
+                      " is current");
+    return NM_ERR_STATE;
+  }
   v.grid = reinterpret_cast<nmg::EscapeValue*>(out);
   v.smooth64 = nullptr;
   NoAllocScratch* s = nullptr;

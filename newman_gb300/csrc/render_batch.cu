@@ -257,6 +257,7 @@ int blocks_of(const void* kernel, int threads, int device) {
 
 template <int kFp64Warps>
 void launch_overlap_with(const BatchLaunch& L, cudaStream_t s) {
+  note_launches(1);
   batch_overlap_kernel<kFp64Warps>
       <<<blocks_of((const void*)batch_overlap_kernel<kFp64Warps>, kPersistentThreads, L.device),
          kPersistentThreads, 0, s>>>(L.fe, L.fe_buf, L.fe_ctl, L.hw, L.hw_ctl, L.overlap_ctl,
@@ -275,6 +276,15 @@ void launch_overlap(const BatchLaunch& L, cudaStream_t s) {
     launch_overlap_with<6>(L, s);
 }
 
+void launch_reduce_all(const BatchLaunch& L, cudaStream_t s) {
+  if (L.nreduce > 0 && L.reduce_total > 0) {
+    long long blocks = (L.reduce_total + 255) / 256;
+    if (blocks > 152 * 64) blocks = 152 * 64;
+    note_launches(1);
+    batch_reduce_kernel<<<(int)blocks, 256, 0, s>>>(L.reduce, L.nreduce, L.reduce_total);
+  }
+}
+
 }  // namespace
 
 cudaError_t launch_batch(const BatchLaunch& L, cudaStream_t s) {
@@ -286,6 +296,7 @@ cudaError_t launch_batch(const BatchLaunch& L, cudaStream_t s) {
                                       (size_t)L.fe.total * sizeof(unsigned int), s);
       if (e != cudaSuccess) return e;
     }
+    note_launches(2);  // the front and the iteration pass
     batch_front_kernel<<<blocks_of((const void*)batch_front_kernel, 256, dev), 256, 0, s>>>(
         L.fe, L.fe_buf, L.fe_ctl.stats);
     if (L.overlap)
@@ -293,25 +304,34 @@ cudaError_t launch_batch(const BatchLaunch& L, cudaStream_t s) {
     else
       batch_iter_kernel<<<blocks_of((const void*)batch_iter_kernel, kPersistentThreads, dev),
                           kPersistentThreads, 0, s>>>(L.fe, L.fe_buf, L.fe_ctl, L.fe_chunk);
+    note_launches(1);
     batch_list_kernel<Fp64AnyJob>
         <<<blocks_of((const void*)batch_list_kernel<Fp64AnyJob>, kPersistentThreads, dev),
            kPersistentThreads, 0, s>>>(L.fe, L.rework_ctl, L.chunk);
   }
   // after an overlapped FE32 pass the double-path range is already used up
   // (its counter is shared), and this launch only checks that
+  if (L.hw.n > 0 && L.hw.total > 0) note_launches(1);
   if (L.hw.n > 0 && L.hw.total > 0)
     batch_list_kernel<HwJob>
         <<<blocks_of((const void*)batch_list_kernel<HwJob>, kPersistentThreads, dev),
            kPersistentThreads, 0, s>>>(L.hw, L.hw_ctl, L.chunk);
+  if (L.fp64.n > 0 && L.fp64.total > 0) note_launches(1);
   if (L.fp64.n > 0 && L.fp64.total > 0)
     batch_list_kernel<Delta64Job>
         <<<blocks_of((const void*)batch_list_kernel<Delta64Job>, kPersistentThreads, dev),
            kPersistentThreads, 0, s>>>(L.fp64, L.fp64_ctl, L.chunk);
-  if (L.nreduce > 0 && L.reduce_total > 0) {
-    long long blocks = (L.reduce_total + 255) / 256;
-    if (blocks > 152 * 64) blocks = 152 * 64;
-    batch_reduce_kernel<<<(int)blocks, 256, 0, s>>>(L.reduce, L.nreduce, L.reduce_total);
-  }
+  launch_reduce_all(L, s);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_rework(const BatchLaunch& L, cudaStream_t s) {
+  if (L.fe.n > 0 && L.fe.total > 0) note_launches(1);
+  if (L.fe.n > 0 && L.fe.total > 0)
+    batch_list_kernel<Fp64AnyJob>
+        <<<blocks_of((const void*)batch_list_kernel<Fp64AnyJob>, kPersistentThreads, L.device),
+           kPersistentThreads, 0, s>>>(L.fe, L.rework_ctl, L.chunk);
+  launch_reduce_all(L, s);
   return cudaGetLastError();
 }
 

@@ -245,6 +245,7 @@ int fe32_blocks_per_sm() {
 
 cudaError_t launch_fe32(const DeviceView& v, const RenderCtl& ctl, cudaStream_t stream,
                         int blocks, int chunk) {
+  note_launches(1);
   fe32_kernel<<<blocks, kPersistentThreads, 0, stream>>>(v, ctl, chunk);
   return cudaGetLastError();
 }
@@ -255,6 +256,7 @@ cudaError_t launch_fe32_passes(const DeviceView& v, const FePassBuffers& b, cons
                                const OverlapCtl* overlap) {
   const long long total = v.total;
   if (total <= 0) return cudaSuccess;
+  note_launches(2);
   fe_front_kernel<<<blocks_for((const void*)fe_front_kernel, 256, device), 256, 0, stream>>>(
       v, b, total, ctl.stats);
   if (iter_begin) cudaEventRecord(iter_begin, stream);

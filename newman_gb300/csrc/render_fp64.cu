@@ -8,6 +8,8 @@
 #include "jobs_fp64.cuh"
 #include "persistent.cuh"
 
+#include <atomic>
+
 namespace nmg {
 
 __global__ void __launch_bounds__(kPersistentThreads) hw_kernel(DeviceView v, RenderCtl ctl,
@@ -37,6 +39,12 @@ int fe32_blocks_per_sm();
 
 int kernel_threads(KernelKind) { return kPersistentThreads; }
 
+namespace {
+std::atomic<long long> g_launches{0};
+}
+void note_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+long long launches_so_far() { return g_launches.load(std::memory_order_relaxed); }
+
 int persistent_blocks(KernelKind kind, int device) {
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
@@ -55,14 +63,14 @@ int persistent_blocks(KernelKind kind, int device) {
 
 cudaError_t launch_render(KernelKind kind, const DeviceView& v, const RenderCtl& ctl,
                           cudaStream_t stream, int blocks, int chunk) {
+  if (kind == KERNEL_FE32) return launch_fe32(v, ctl, stream, blocks, chunk);
+  note_launches(1);
   if (kind == KERNEL_HW)
     hw_kernel<<<blocks, kPersistentThreads, 0, stream>>>(v, ctl, chunk);
   else if (kind == KERNEL_DELTA64)
     delta64_kernel<<<blocks, kPersistentThreads, 0, stream>>>(v, ctl, chunk);
-  else if (kind == KERNEL_REWORK)
-    rework_kernel<<<blocks, kPersistentThreads, 0, stream>>>(v, ctl, chunk);
   else
-    return launch_fe32(v, ctl, stream, blocks, chunk);
+    rework_kernel<<<blocks, kPersistentThreads, 0, stream>>>(v, ctl, chunk);
   return cudaGetLastError();
 }
 
@@ -107,12 +115,14 @@ static int grid_for(long long n) {
 
 cudaError_t launch_reduce(const EscapeValue* in, int nr, int nc, int sc, EscapeValue* out,
                           cudaStream_t stream) {
+  note_launches(1);
   reduce_kernel<<<grid_for((long long)nr * nc), 256, 0, stream>>>(in, nr, nc, sc, out);
   return cudaGetLastError();
 }
 
 cudaError_t launch_duplicate(const EscapeValue* in, int nr, int nc, int sc, EscapeValue* out,
                              cudaStream_t stream) {
+  note_launches(1);
   duplicate_kernel<<<grid_for((long long)nr * nc * sc * sc), 256, 0, stream>>>(in, nr, nc, sc,
                                                                                  out);
   return cudaGetLastError();

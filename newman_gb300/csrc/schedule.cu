@@ -313,6 +313,7 @@ namespace {
 using nmg::fail;
 
 int upload_to_half(nm_costmodel* m) {
+  nmg::note_launches(1);
   nmg::to_half_kernel<<<(nmg::kParams + 255) / 256, 256, 0, m->stream>>>(m->params.p, m->wh.p);
   NM_CUDA(cudaGetLastError());
   return NM_OK;
@@ -333,6 +334,7 @@ int launch_mlp(nm_costmodel* m, int n, float* out) {
   const size_t smem = sizeof(nmg::MlpShared);
   NM_CUDA(cudaFuncSetAttribute(nmg::mlp_kernel<kTrain>,
                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  nmg::note_launches(1);
   nmg::mlp_kernel<kTrain><<<nmg::mlp_blocks(n, m->device), nmg::kH, smem, m->stream>>>(
       m->wh.p, m->params.p, m->x.p, kTrain ? m->t.p : nullptr, n, out, m->grad.p,
       m->scratch.p);
@@ -441,6 +443,7 @@ int nm_cost_model_train(nm_costmodel* m, const float* x, const float* t, int n, 
     m->step++;
     const float b1t = (float)std::pow(0.9, (double)m->step);
     const float b2t = (float)std::pow(0.999, (double)m->step);
+    nmg::note_launches(1);
     nmg::adam_kernel<<<(nmg::kParams + 255) / 256, 256, 0, m->stream>>>(
         m->params.p, m->grad.p, m->m.p, m->v.p, m->wh.p, lr, b1t, b2t);
     NM_CUDA(cudaGetLastError());
@@ -468,6 +471,7 @@ int nm_tile_features(nm_handle* preview, int tile_w, int tile_h, float* out, int
   NM_CUDA(cudaMemcpyAsync(lohi.p, init, 8, cudaMemcpyHostToDevice, s));
   const long long n = (long long)nr * nc;
   const int N = preview->view.iterations();
+  nmg::note_launches(2);
   nmg::preview_range_kernel<<<256, 256, 0, s>>>(preview->grid.p, n, N, lohi.p);
   nmg::tile_features_kernel<<<(ntiles + 127) / 128, 128, 0, s>>>(
       preview->grid.p, nr, nc, N, tile_w, tile_h, tx, ntiles, lohi.p, d_out.p);

@@ -138,6 +138,7 @@ extern "C" int nm_video_interpolate(const unsigned char* prev_rgb, const unsigne
   const long long n = (long long)rate * rows * cols;
   long long blocks = (n + 255) / 256;
   if (blocks > 152 * 64) blocks = 152 * 64;
+  nmg::note_launches(1);
   nmg::interp_kernel<<<(int)blocks, 256>>>(d_prev.p, d_cur.p, key_rows, key_cols, rows, cols,
                                            d_geom.p, rate, d_out.p);
   NM_CUDA(cudaGetLastError());

@@ -118,3 +118,36 @@ def test_batch_with_fe32_double_loop_frames(nm):
             dl = make_frame(nm, v, 2, nm.PATH_FE32)
             dl.render()
             assert (dl.grid()["iterations"] == alone.grid()["iterations"]).mean() >= 0.9999
+
+
+def test_batch_rebuilds_after_a_frame_changes(nm):
+    """A frame whose view changes after the batch captured its graph (N here,
+    re-precomputed and re-uploaded into buffers of the same size, so that no
+    device pointer moves) must be rendered with its new tables, not replayed
+    from the old graph."""
+    views = zoom_frames(4, 64, 96, "1e-3", "1e-40", 2000, 8000)
+    frames = [make_frame(nm, v, 2, nm.PATH_FE32) for v in views]
+    for f in frames:
+        f.precompute()
+        f.upload()
+    batch = nm.Batch(sc=2)
+    for f in frames:
+        batch.add(f)
+    batch.render()
+    k = len(frames) - 1
+    grid_before = frames[k].device_grid()
+    frames[k].N = 3000
+    frames[k].precompute()
+    frames[k].upload()
+    assert frames[k].device_grid() == grid_before  # same buffers: pointers cannot tell
+    batch.render()
+    got = batch.frames_out()
+    for j, v in enumerate(views):
+        alone = make_frame(nm, v, 2, nm.PATH_FE32)
+        if j == k:
+            alone.N = 3000
+        alone.precompute()
+        alone.render()
+        ref = alone.reduce(2)
+        assert np.array_equal(got[j]["iterations"], ref["iterations"]), "frame %d" % j
+    assert int(got[k]["iterations"].max()) <= 3000

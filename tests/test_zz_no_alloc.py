@@ -68,3 +68,30 @@ def test_noalloc_refuses_oversize_and_unprepared(nm):
     with pytest.raises(nm.NewmanError) as e:
         small.render_noalloc(ctypes.c_void_p(1))
     assert e.value.code == nm.NM_ERR_STATE
+
+
+@pytest.mark.parametrize("width", ["1e-8", "6e-8"])
+def test_noalloc_on_double_loop_views(nm, width):
+    """Views where the reference takes its double loop: at a sample step below
+    2^-33 (width 1e-8 on 240 columns) the FE32 path renders them with the
+    double loop itself; above it (6e-8) with FE32 perturbation certified
+    against the double loop, reworked by it.  Both through the allocation-free
+    entry point must give nm_render's escape counts on the same handle."""
+    torch = pytest.importorskip("torch")
+    view = dict(shrink(C2, 90, 120, N=6000), step=step_for(width, 240), sc=2)
+    m = setup_gpu(nm, view, path=nm.PATH_FE32, keep64=False)
+    assert m.useHardware()
+    m.precompute()
+    m.upload()
+    m.render()
+    ref = m.grid().copy()
+    rows, cols = m.rows(), m.cols()
+    out = torch.empty(rows * cols * 2, dtype=torch.int32, device="cuda")
+    stream = torch.cuda.current_stream()
+    for call in range(2):
+        out.fill_(-7)
+        m.render_noalloc(ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(stream.cuda_stream))
+        stream.synchronize()
+        got = out.cpu().numpy().view(nm.ESCAPE_DTYPE).reshape(rows, cols)
+        assert np.array_equal(got["iterations"], ref["iterations"]), "call %d" % call
+        assert np.abs(got["smoothing"] - ref["smoothing"]).max() <= 1e-6, "call %d" % call

@@ -220,11 +220,11 @@ def cpu_reference(seconds, threads, seed=7):
     return total_it / elapsed, total_px, threads
 
 
-def reference_agreement(nm, m, fp, n_samples, seed=11):
-    """Escape counts of the FE32 grid (m) and the FP64 grid (fp) against the
-    reference's own semantics -- getIterations with its arbitrary-precision
-    continuation (the oracle's MODE_REF) -- on a seeded random sample of the
-    workload's samples, on all host threads."""
+def reference_agreement(nm, grids, n_samples, seed=11):
+    """Escape counts of the grids (name -> escape-count array of the
+    workload) against the reference's own semantics -- getIterations with its
+    arbitrary-precision continuation (the oracle's MODE_REF) -- on a seeded
+    random sample of the workload's samples, on all host threads."""
     from oracle import oracle
     threads = os.cpu_count() or 1
     o = oracle.OracleView(NR, NC)
@@ -240,10 +240,40 @@ def reference_agreement(nm, m, fp, n_samples, seed=11):
     cpu_s = time.perf_counter() - t0
     out = {"samples": int(n_samples), "seed": seed, "oracle": "MODE_REF (MP continuation)",
            "cpu_s": cpu_s, "threads": threads}
-    for name, g in (("fe32", m), ("fp64", fp)):
-        gi = g[rr, cc]
-        out["exact_" + name] = float((gi == it).mean())
+    for name, g in grids.items():
+        out["exact_" + name] = float((g[rr, cc] == it).mean())
     return out
+
+
+def mp_path(nm, stream, flush):
+    """The reference-exact path on the same workload: the reference's series
+    front and its arbitrary-precision continuation with GMP mpf's truncations
+    reproduced on the GPU; one render timed (device time, L2 flushed)."""
+    m = nm.Mandelbrot(NR, NC)
+    m.set_view(CENTER[0], CENTER[1], step_string(), step_string(), N_ITER, TOL)
+    m.scaleUp(SC)
+    m.set_path(nm.PATH_MP)
+    m.precompute()
+    m.upload()
+    times = []
+    for i in range(2):
+        with torch_stream(stream):
+            flush.zero_()
+        e0, e1 = cuda_events()
+        e0.record(stream)
+        m.render_rows(0, m.rows(), stream.cuda_stream)
+        e1.record(stream)
+        m.synchronize()
+        stream.synchronize()
+        if i:
+            times.append(e0.elapsed_time(e1))
+    ms = float(np.mean(times))
+    g = m.grid()["iterations"]
+    eff = int(g.astype(np.int64).sum())
+    executed = m.stat(nm.STAT_EXECUTED_ITERS)
+    return {"ms": ms, "value": eff / (ms * 1e-3), "unit": "pixel-iters/s",
+            "executed_iters": executed, "executed_iters_per_s": executed / (ms * 1e-3),
+            "precision_bits": m.stat(nm.STAT_PRECISION_BITS)}, g
 
 
 def c3_deep(nm, steps, flush, stream):
@@ -447,9 +477,14 @@ def run_ours(args):
     red_fe = m.reduce(SC)
     red_fp = fp.reduce(SC)
     exact_px = float((red_fe["iterations"] == red_fp["iterations"]).mean())
-    agreement = None
+    agreement, mp_line = None, None
+    if rank == 0 and not args.no_mp:
+        mp_line, g_mp = mp_path(nm, stream, flush)
     if rank == 0 and not args.no_cpu and args.ref_samples > 0:
-        agreement = reference_agreement(nm, g["iterations"], gf["iterations"], args.ref_samples)
+        grids = {"fe32": g["iterations"], "fp64": gf["iterations"]}
+        if mp_line is not None:
+            grids["mp"] = g_mp
+        agreement = reference_agreement(nm, grids, args.ref_samples)
     del gf, dsm, same
 
     # e2e through the C ABI with host buffers, as the reference renders a view
@@ -527,6 +562,7 @@ def run_ours(args):
                     "includes": "nm_precompute (host probe search, orbit, series), table "
                                 "upload, render, reduce, reduced grid to host; L2 flushed"},
             "exact_vs_reference_mp": agreement,
+            "mp_path": mp_line,
         }
         if not args.no_cpu:
             v, px, cores = cpu_reference(args.cpu_seconds, 1)
@@ -910,6 +946,8 @@ def main():
     ap.add_argument("--path", default="fe32", choices=["fe32", "fp64"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-mp", action="store_true",
+                    help="leave out the reference-exact path's render of the workload")
     ap.add_argument("--no-deep", action="store_true",
                     help="leave out the 3840x2160 width-1e-300 comparison of the default line")
     ap.add_argument("--ref-samples", type=int, default=100000,

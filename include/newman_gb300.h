@@ -51,7 +51,16 @@ enum nm_path {
   /* Plain FP64 perturbation: series skip, then FP64 delta iteration. */
   NM_PATH_FP64 = 1,
   /* FP32 mantissa + int exponent delta iteration (floatexp). */
-  NM_PATH_FE32 = 2
+  NM_PATH_FE32 = 2,
+  /* The reference's own arithmetic, bit for bit: where useHardware() holds
+     its double loop, else its series front in doubles followed by the
+     arbitrary-precision continuation of getIterations (mandelbrot.cpp:209-224)
+     with GMP mpf's truncations reproduced on the GPU; the cardioid test in
+     the view's precision in both.  Views of 64 to 448 bits of precision
+     whose series stays in the double range (where the reference renders at
+     all); others are refused with NM_ERR_UNSUPPORTED.  Choose it before
+     nm_precompute, which then keeps the orbit in arbitrary precision. */
+  NM_PATH_MP = 3
 };
 
 enum nm_option {

@@ -18,7 +18,7 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libnewman_gb300.so")
 # include/newman_gb300.h
 NM_OK, NM_ERR_ARG, NM_ERR_PARSE, NM_ERR_STATE, NM_ERR_CUDA, NM_ERR_CANCELLED, NM_ERR_IO, \
     NM_ERR_UNSUPPORTED = range(8)
-PATH_REFERENCE, PATH_FP64, PATH_FE32 = 0, 1, 2
+PATH_REFERENCE, PATH_FP64, PATH_FE32, PATH_MP = 0, 1, 2, 3
 OPT_TILE_W, OPT_TILE_H, OPT_CHUNK, OPT_KEEP_SMOOTH64, OPT_THREADS, OPT_BLOCKS, OPT_RENORM, \
     OPT_FE32_SINGLE_PASS, OPT_REFERENCE, OPT_BATCH_GRAPH, OPT_FE32_OVERLAP, \
     OPT_LOG_TILE_COSTS, OPT_BATCH_FP64_WARPS = range(13)

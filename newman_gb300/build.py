@@ -22,6 +22,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # Per-file nvcc flags: the FP64 reference-order kernels never contract.
 CU_FLAGS = {
     "render_fp64.cu": ["--fmad=false"],
+    "render_mp.cu": ["--fmad=false"],
 }
 
 

@@ -124,6 +124,12 @@ int ensure_coords(nm_handle* h) {
   for (size_t i = 0; i < re.size(); i++) h->coord_re[i] = {re[i].x, re[i].y};
   for (size_t i = 0; i < im.size(); i++) h->coord_im[i] = {im[i].x, im[i].y};
   h->outside_cardioid = h->view.view_outside_cardioid();
+  if (h->path == NM_PATH_MP) {
+    h->view.coordinates_mp(h->coord_re_mp, h->coord_im_mp);
+  } else {
+    h->coord_re_mp.clear();
+    h->coord_im_mp.clear();
+  }
   h->coords_valid = true;
   h->uploaded = false;
   return NM_OK;
@@ -134,6 +140,12 @@ int do_upload(nm_handle* h) {
   if ((rc = ensure_device(h))) return rc;
   if ((rc = upload(h->d_coord_re, h->coord_re, h->stream))) return rc;
   if ((rc = upload(h->d_coord_im, h->coord_im, h->stream))) return rc;
+  if (!h->coord_re_mp.empty()) {
+    if ((rc = upload(h->d_coord_re_mp, h->coord_re_mp, h->stream))) return rc;
+    if ((rc = upload(h->d_coord_im_mp, h->coord_im_mp, h->stream))) return rc;
+  }
+  if (h->precomputed && !h->od.xmp.empty())
+    if ((rc = upload(h->d_x_mp, h->od.xmp, h->stream))) return rc;
   if (h->precomputed) {
     auto cv = [](const std::vector<nmg::D2>& v) {
       std::vector<Dbl2> o(v.size());
@@ -274,8 +286,20 @@ void set_fe_tables(const nm_handle* h, nmg::DeviceView& v) {
 
 int nmg::prepare_view(nm_handle* h, int r0, int r1, nmg::DeviceView& v, nmg::KernelKind& kind) {
   const int nr = h->view.rows(), nc = h->view.cols();
-  const bool hw =
-      h->view.use_hardware() && (h->path == NM_PATH_REFERENCE || double_loop_direct(h));
+  const bool hw = h->view.use_hardware() &&
+                  (h->path == NM_PATH_REFERENCE || h->path == NM_PATH_MP || double_loop_direct(h));
+  const int mp_limbs = nmg::mp_limbs_for_bits(h->view.bits());
+  if (h->path == NM_PATH_MP) {
+    if (mp_limbs < nmg::kMpMinLimbs || mp_limbs > nmg::kMpMaxLimbs)
+      return fail(NM_ERR_UNSUPPORTED, "the reference-exact path takes 64 to %d bits of precision "
+                  "(the view has %lu)", 64 * (nmg::kMpMaxLimbs - 2), h->view.bits());
+    if (!hw && h->precomputed && h->od.mp_limbs != mp_limbs)
+      return fail(NM_ERR_STATE, "precomputed without the arbitrary-precision orbit; "
+                                "nm_precompute again after choosing NM_PATH_MP");
+    if (!hw && h->precomputed && !h->od.sa_fp64_ok)
+      return fail(NM_ERR_UNSUPPORTED, "the reference-exact path needs series terms in the double "
+                                      "range (the reference renders no other view)");
+  }
   if (!hw && !h->precomputed)
     return fail(NM_ERR_STATE, "deep view: nm_precompute must run before rendering");
   if (!hw && h->od.double_loop && h->path != NM_PATH_FE32)
@@ -336,6 +360,14 @@ int nmg::prepare_view(nm_handle* h, int r0, int r1, nmg::DeviceView& v, nmg::Ker
     }
     v.tile_order = h->d_tile_order.p;
   }
+  if (h->path == NM_PATH_MP) {
+    v.mp_limbs = mp_limbs;
+    v.coord_re_mp = h->d_coord_re_mp.p;
+    v.coord_im_mp = h->d_coord_im_mp.p;
+    v.x_mp = hw ? nullptr : h->d_x_mp.p;
+    kind = hw ? nmg::KERNEL_HW_MP : nmg::KERNEL_MP;
+    return NM_OK;
+  }
   kind = hw ? nmg::KERNEL_HW : (h->path == NM_PATH_FE32 ? nmg::KERNEL_FE32 : nmg::KERNEL_DELTA64);
   return NM_OK;
 }
@@ -371,6 +403,8 @@ nm_handle* nm_copy(const nm_handle* src) {
   h->keep_smooth64 = src->keep_smooth64;
   h->coord_re = src->coord_re;
   h->coord_im = src->coord_im;
+  h->coord_re_mp = src->coord_re_mp;
+  h->coord_im_mp = src->coord_im_mp;
   h->eps_re = src->eps_re;
   h->eps_im = src->eps_im;
   h->eps_re_fe = src->eps_re_fe;
@@ -463,7 +497,11 @@ int nm_use_hardware(const nm_handle* h) { return h ? (h->view.use_hardware() ? 1
 
 int nm_set_path(nm_handle* h, int path) {
   if (int rc = check_handle(h)) return rc;
-  if (path < NM_PATH_REFERENCE || path > NM_PATH_FE32) return fail(NM_ERR_ARG, "bad path %d", path);
+  if (path < NM_PATH_REFERENCE || path > NM_PATH_MP) return fail(NM_ERR_ARG, "bad path %d", path);
+  if ((path == NM_PATH_MP) != (h->path == NM_PATH_MP)) {
+    h->coords_valid = false;  // the arbitrary-precision coordinate tables come and go
+    h->uploaded = false;
+  }
   h->path = path;
   h->generation++;
   return NM_OK;
@@ -576,9 +614,10 @@ int nm_precompute(nm_handle* h) {
     for (size_t r = 0; r < py.size(); r++) py[r] = h->coord_im[r].x;
     h->view.eps_tables_double_loop(px, py, h->eps_re, h->eps_im);
     h->precomputed = true;
-  } else if (!h->view.use_hardware() || h->path != NM_PATH_REFERENCE) {
+  } else if (!h->view.use_hardware() ||
+             (h->path != NM_PATH_REFERENCE && h->path != NM_PATH_MP)) {
     int threads = h->threads > 0 ? h->threads : (int)std::thread::hardware_concurrency();
-    if (h->view.precompute(threads, h->od, h->reference_mode))
+    if (h->view.precompute(threads, h->od, h->reference_mode, h->path == NM_PATH_MP))
       return fail(NM_ERR_STATE, "precompute failed");
     h->view.eps_tables(h->od, h->eps_re, h->eps_im);
     if (!h->od.sa_fp64_ok) h->view.eps_tables_fe(h->eps_re_fe, h->eps_im_fe);

@@ -37,7 +37,23 @@ struct RenderCtl {
 
 // KERNEL_REWORK: the FE32 path's FP64 rework (the double loop on double-loop
 // views, else the FP64 delta path).
-enum KernelKind { KERNEL_HW = 0, KERNEL_DELTA64 = 1, KERNEL_FE32 = 2, KERNEL_REWORK = 3 };
+// KERNEL_MP: the reference-exact path (the series front, then the reference's
+// arbitrary-precision continuation in its own arithmetic, mpf_fixed.cuh);
+// KERNEL_HW_MP: the double loop with the cardioid test in that arithmetic.
+enum KernelKind {
+  KERNEL_HW = 0,
+  KERNEL_DELTA64 = 1,
+  KERNEL_FE32 = 2,
+  KERNEL_REWORK = 3,
+  KERNEL_MP = 4,
+  KERNEL_HW_MP = 5
+};
+// Precisions the reference-exact kernels are built for: values of
+// kMpMinLimbs .. kMpMaxLimbs limbs (GMP precisions of 64 .. 64 (kMpMaxLimbs - 2)
+// bits).
+constexpr int kMpMinLimbs = 3, kMpMaxLimbs = 9;
+cudaError_t launch_mp(KernelKind kind, const DeviceView& v, const RenderCtl& ctl,
+                      cudaStream_t stream, int blocks, int chunk);
 
 // Buffers of the FE32 pass pipeline (render_fe32.cu), one record per sample
 // index in tile order.

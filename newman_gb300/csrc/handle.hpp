@@ -125,6 +125,9 @@ struct nm_handle {
   bool fe_overlap = true;       // FE32 passes: FP64 rework inside the iteration pass
   DevBuf<char> d_fe_state;
   DevBuf<nmg::FeTrap> d_fe_trap;  // double-loop views on the FE32 path
+  // the reference-exact path: sample coordinates in arbitrary precision
+  std::vector<uint64_t> coord_re_mp, coord_im_mp;
+  DevBuf<uint64_t> d_coord_re_mp, d_coord_im_mp, d_x_mp;
   DevBuf<unsigned int> d_work;
 
   // scheduling: the order in which whole-grid renders hand out their tiles (a

@@ -1,0 +1,408 @@
+// Arbitrary-precision floats with the results of GMP's mpf functions, at a
+// precision fixed at compile time -- for the GPU (and the host) to continue
+// the reference's per-pixel iteration in the arbitrary precision it uses
+// (mandelbrot.cpp:209-224, the gmpxx expressions of complex.h and :102-103)
+// and get the same bits.
+//
+// GMP's mpf functions do not round correctly: each truncates its operands at
+// limb boundaries that depend on the destination's precision, then truncates
+// the result.  What they compute, for a destination of P limbs of precision
+// (GMP's _mp_prec; mpf_init2(x, bits) gives P = (bits + 127) / 64, and a value
+// holds up to P + 1 limbs), was established here by calling GMP 6.3.0
+// (libgmp.so.10) on millions of structured random operands and comparing
+// values limb for limb (tests/native/mpf_conformance.cpp keeps that check):
+//
+//   mul(u, v)  both operands cut to their top P limbs, exact product, cut to
+//              its top P + 1 limbs;
+//   add(u, v)  same signs: both cut at limb position E - P, E the larger
+//              exponent, exact sum (P + 1 limbs when it carries);
+//              opposite signs: leading limbs that cancel exactly are skipped
+//              first -- limbs equal in both (equal exponents), then a
+//              difference of 1 followed by limb pairs (0, 2^64 - 1), which
+//              cancel to a 1 one limb lower -- and both operands are cut
+//              P + 1 limbs below the position so reached; exact difference;
+//   get_d(x)   x truncated toward zero to a double;
+//   set_d(x)   exact.
+//
+// A value is sign, limb exponent e and the D = P + 1 limbs d[0..P], most
+// significant first, value = sign * sum_i d[i] * 2^(64 (e - 1 - i)), with
+// d[0] != 0 unless the value is 0.  Limbs below the value's own are zero;
+// trailing zero limbs never change a result (every cut is at a limb position
+// fixed by exponents and operand values, not by limb counts).
+#pragma once
+
+#include <cstdint>
+
+#if defined(__CUDACC__)
+#define MPF_HD __host__ __device__ __forceinline__
+#else
+#define MPF_HD inline
+#endif
+
+namespace nmg {
+
+template <int P>
+struct Mpf {
+  static_assert(P >= 2, "GMP's smallest mpf precision is 2 limbs (64 bits)");
+  static constexpr int D = P + 1;
+  uint64_t d[D];
+  int32_t e;
+  int32_t s;  // -1, 0, +1
+};
+
+namespace mpf_detail {
+
+MPF_HD void mul64(uint64_t a, uint64_t b, uint64_t& lo, uint64_t& hi) {
+#if defined(__CUDA_ARCH__)
+  lo = a * b;
+  hi = __umul64hi(a, b);
+#else
+  const unsigned __int128 p = (unsigned __int128)a * b;
+  lo = (uint64_t)p;
+  hi = (uint64_t)(p >> 64);
+#endif
+}
+
+MPF_HD int clz64(uint64_t x) {
+#if defined(__CUDA_ARCH__)
+  return __clzll((long long)x);
+#else
+  return x ? __builtin_clzll(x) : 64;
+#endif
+}
+
+// a + b + c (c in {0, 1}); c becomes the carry out.
+MPF_HD uint64_t addc(uint64_t a, uint64_t b, uint64_t& c) {
+  const uint64_t t = a + b;
+  const uint64_t c1 = t < a;
+  const uint64_t u = t + c;
+  c = c1 | (uint64_t)(u < t);
+  return u;
+}
+
+// a - b - br (br in {0, 1}); br becomes the borrow out.
+MPF_HD uint64_t subb(uint64_t a, uint64_t b, uint64_t& br) {
+  const uint64_t t = a - b;
+  const uint64_t b1 = a < b;
+  const uint64_t u = t - br;
+  br = b1 | (uint64_t)(t < br);
+  return u;
+}
+
+// d[k] for a runtime k, 0 outside [0, D): selects over the limbs, so that the
+// limbs stay in registers on the GPU.
+template <int D>
+MPF_HD uint64_t limb_at(const uint64_t (&d)[D], int k) {
+  uint64_t r = 0;
+#pragma unroll
+  for (int j = 0; j < D; j++) r = (k == j) ? d[j] : r;
+  return r;
+}
+
+}  // namespace mpf_detail
+
+template <int P>
+MPF_HD Mpf<P> mpf_zero() {
+  Mpf<P> r;
+#pragma unroll
+  for (int i = 0; i < Mpf<P>::D; i++) r.d[i] = 0;
+  r.e = 0;
+  r.s = 0;
+  return r;
+}
+
+template <int P>
+MPF_HD Mpf<P> mpf_neg(Mpf<P> a) {
+  a.s = -a.s;
+  return a;
+}
+
+// -1, 0, 1 as |a| is below, equal to or above |b|.
+template <int P>
+MPF_HD int mpf_cmp_abs(const Mpf<P>& a, const Mpf<P>& b) {
+  if (a.s == 0 || b.s == 0) return (a.s != 0) - (b.s != 0);
+  if (a.e != b.e) return a.e < b.e ? -1 : 1;
+  int r = 0;
+#pragma unroll
+  for (int i = 0; i < Mpf<P>::D; i++)
+    if (r == 0 && a.d[i] != b.d[i]) r = a.d[i] < b.d[i] ? -1 : 1;
+  return r;
+}
+
+// mpf_cmp: -1, 0, 1 as a is below, equal to or above b.
+template <int P>
+MPF_HD int mpf_cmp(const Mpf<P>& a, const Mpf<P>& b) {
+  if (a.s != b.s) return a.s < b.s ? -1 : 1;
+  const int m = mpf_cmp_abs(a, b);
+  return a.s < 0 ? -m : m;
+}
+
+// mpf_mul into a destination of P limbs of precision.
+template <int P>
+MPF_HD Mpf<P> mpf_mul(const Mpf<P>& a, const Mpf<P>& b) {
+  using namespace mpf_detail;
+  constexpr int D = P + 1;
+  if (a.s == 0 || b.s == 0) return mpf_zero<P>();
+  // the top P limbs of each, little-endian, and their exact product
+  uint64_t r[2 * P];
+#pragma unroll
+  for (int k = 0; k < 2 * P; k++) r[k] = 0;
+#pragma unroll
+  for (int i = 0; i < P; i++) {
+    const uint64_t ai = a.d[P - 1 - i];
+    uint64_t carry = 0;
+#pragma unroll
+    for (int j = 0; j < P; j++) {
+      uint64_t lo, hi;
+      mul64(ai, b.d[P - 1 - j], lo, hi);
+      uint64_t c = 0;
+      lo = addc(lo, r[i + j], c);
+      hi += c;
+      c = 0;
+      lo = addc(lo, carry, c);
+      hi += c;
+      r[i + j] = lo;
+      carry = hi;
+    }
+    r[i + P] = carry;
+  }
+  // top limb zero: one limb lower
+  const bool adj = r[2 * P - 1] == 0;
+  Mpf<P> o;
+#pragma unroll
+  for (int k = 0; k < D; k++) {
+    const uint64_t hi = r[2 * P - 1 - k];
+    const uint64_t lo = (2 * P - 2 - k >= 0) ? r[(2 * P - 2 - k) >= 0 ? 2 * P - 2 - k : 0] : 0;
+    o.d[k] = adj ? lo : hi;
+  }
+  o.e = a.e + b.e - (adj ? 1 : 0);
+  o.s = a.s * b.s;
+  return o;
+}
+
+// mpf_mul(r, two, a) with two = 2.0: 2 times the top P limbs of a, exactly.
+template <int P>
+MPF_HD Mpf<P> mpf_mul2(const Mpf<P>& a) {
+  constexpr int D = P + 1;
+  if (a.s == 0) return a;
+  Mpf<P> o;
+  const uint64_t top = a.d[0] >> 63;
+  if (top) {  // the product gains a limb
+    o.d[0] = 1;
+#pragma unroll
+    for (int k = 1; k < D; k++)
+      o.d[k] = (a.d[k - 1] << 1) | ((k < P) ? (a.d[k < P ? k : 0] >> 63) : 0);
+    o.e = a.e + 1;
+  } else {
+#pragma unroll
+    for (int k = 0; k < D; k++)
+      o.d[k] = (k < P) ? ((a.d[k < P ? k : 0] << 1) | ((k + 1 < P) ? (a.d[k + 1 < P ? k + 1 : 0] >> 63) : 0))
+                       : 0;
+    o.e = a.e;
+  }
+  o.s = a.s;
+  return o;
+}
+
+// mpf_add (and mpf_sub = mpf_add with -b) into a destination of P limbs.
+template <int P>
+MPF_HD Mpf<P> mpf_add(const Mpf<P>& a, const Mpf<P>& b) {
+  using namespace mpf_detail;
+  constexpr int D = P + 1;
+  if (a.s == 0) return b;
+  if (b.s == 0) return a;
+  Mpf<P> o;
+  if (a.s == b.s) {
+    // both cut at limb position E - P: the top P limbs below E
+    const bool a_hi = a.e >= b.e;
+    const Mpf<P>& u = a_hi ? a : b;
+    const Mpf<P>& v = a_hi ? b : a;
+    const int off = u.e - v.e;  // v's limb k sits at u's index k + off
+    uint64_t sum[P];
+    uint64_t c = 0;
+#pragma unroll
+    for (int i = P - 1; i >= 0; i--) sum[i] = addc(u.d[i], limb_at(v.d, i - off), c);
+    if (c) {
+      o.d[0] = 1;
+#pragma unroll
+      for (int k = 1; k < D; k++) o.d[k] = sum[k - 1];
+      o.e = u.e + 1;
+    } else {
+#pragma unroll
+      for (int k = 0; k < P; k++) o.d[k] = sum[k];
+      o.d[P] = 0;
+      o.e = u.e;
+    }
+    o.s = u.s;
+    return o;
+  }
+  // opposite signs: U the larger magnitude
+  const int m = mpf_cmp_abs(a, b);
+  if (m == 0) return mpf_zero<P>();
+  const Mpf<P>& U = m > 0 ? a : b;
+  const Mpf<P>& W = m > 0 ? b : a;
+  const int off = U.e - W.e;  // W's limb k sits at U's index k + off; off >= 0
+  // first index where the limbs differ (equal exponents: equal leading limbs
+  // cancel)
+  int t = 0;
+  if (off == 0) {
+    bool eq = true;
+#pragma unroll
+    for (int i = 0; i < D; i++) {
+      eq = eq && U.d[i] == W.d[i];
+      t += eq ? 1 : 0;
+    }
+  }
+  // U[t] - W[t] == 1 followed by (0, 2^64 - 1) pairs: they cancel to a 1 at
+  // the last pair's index
+  const uint64_t ut = limb_at(U.d, t), wt = limb_at(W.d, t - off);
+  int s0 = t;
+  uint64_t topw = ut - wt;
+  if (topw == 1) {
+    int j = t + 1;
+    // bounded: W's limbs end D + off indexes down
+    for (int k = 0; k < D + 1; k++) {
+      if (limb_at(U.d, j) == 0 && limb_at(W.d, j - off) == ~0ull)
+        j++;
+      else
+        break;
+    }
+    s0 = j - 1;
+  }
+  // window of D limbs from index s0: the top word is topw (1 after a chain),
+  // the D - 1 below are U - W with borrows
+  uint64_t w[D];
+  uint64_t br = 0;
+#pragma unroll
+  for (int i = D - 1; i >= 1; i--) w[i] = subb(limb_at(U.d, s0 + i), limb_at(W.d, s0 + i - off), br);
+  w[0] = topw - br;
+  // normalise: leading zero limbs
+  int z = 0;
+  bool lead = true;
+#pragma unroll
+  for (int i = 0; i < D; i++) {
+    lead = lead && w[i] == 0;
+    z += lead ? 1 : 0;
+  }
+  if (z == D) return mpf_zero<P>();
+#pragma unroll
+  for (int k = 0; k < D; k++) o.d[k] = limb_at(w, k + z);
+  o.e = U.e - s0 - z;
+  o.s = U.s;
+  return o;
+}
+
+template <int P>
+MPF_HD Mpf<P> mpf_sub(const Mpf<P>& a, const Mpf<P>& b) {
+  return mpf_add(a, mpf_neg(b));
+}
+
+// mpf_get_d: truncation toward zero (values in the normal double range).
+template <int P>
+MPF_HD double mpf_get_d(const Mpf<P>& a) {
+  using namespace mpf_detail;
+  if (a.s == 0) return 0.0;
+  const int lz = clz64(a.d[0]);
+  uint64_t m = a.d[0] << lz;
+  if (lz) m |= a.d[1] >> (64 - lz);
+  m >>= 11;  // the top 53 bits
+  const int e2 = 64 * (a.e - 1) + (63 - lz) - 52;  // value = m * 2^e2
+  // m * 2^e2 with m < 2^53: exact while the result is a normal double
+  double x = (double)m;
+  int k = e2;
+  // scale by powers of two in steps that stay exact
+  while (k > 900) {
+    x *= 0x1p900;
+    k -= 900;
+  }
+  while (k < -900) {
+    x *= 0x1p-900;
+    k += 900;
+  }
+  union {
+    double f;
+    uint64_t u;
+  } sc;
+  sc.u = (uint64_t)(k + 1023) << 52;
+  x *= sc.f;
+  return a.s < 0 ? -x : x;
+}
+
+// mpf_set_d: a finite double exactly.
+template <int P>
+MPF_HD Mpf<P> mpf_from_double(double x) {
+  Mpf<P> o = mpf_zero<P>();
+  if (x == 0.0) return o;
+  union {
+    double f;
+    uint64_t u;
+  } b;
+  b.f = x;
+  o.s = (b.u >> 63) ? -1 : 1;
+  int be = (int)((b.u >> 52) & 0x7ff);
+  uint64_t m = b.u & ((1ull << 52) - 1);
+  if (be) {
+    m |= 1ull << 52;
+  } else {
+    be = 1;  // subnormal
+  }
+  // value = m * 2^(be - 1075); top bit of m at bit h
+  const int h = 63 - mpf_detail::clz64(m);
+  const int top = be - 1075 + h;        // weight 2^top of the leading bit
+  const int e = (top >> 6) + 1;         // limb exponent (floor division)
+  const int bit = top - 64 * (e - 1);   // leading bit's place in limb e - 1
+  const int sh = bit - h;               // m's bit 0 lands at this bit of limb e - 1
+  if (sh >= 0) {
+    o.d[0] = m << sh;
+  } else {
+    o.d[0] = m >> (-sh);
+    o.d[1] = m << (64 + sh);
+  }
+  o.e = e;
+  return o;
+}
+
+// ---- the reference's arbitrary-precision step, gmpxx order -----------------
+// computeOrbit / getIterations (mandelbrot.cpp:102-103, :213-214):
+//   re = X.re * X.re - X.im * X.im + X0.re;   im = 2.0 * (X.re * X.im) + X0.im
+template <int P>
+MPF_HD void mpf_orbit_step(const Mpf<P>& xr, const Mpf<P>& xi, const Mpf<P>& x0r,
+                           const Mpf<P>& x0i, Mpf<P>& nr, Mpf<P>& ni) {
+  const Mpf<P> t1 = mpf_sub(mpf_mul(xr, xr), mpf_mul(xi, xi));
+  const Mpf<P> t3 = mpf_mul2(mpf_mul(xr, xi));
+  nr = mpf_add(t1, x0r);
+  ni = mpf_add(t3, x0i);
+}
+
+// bailedOut (mandelbrot.cpp:58-61): sqMag(descend(z)) > 1024^2 in doubles,
+// unfused.
+template <int P>
+MPF_HD bool mpf_bailed_out(const Mpf<P>& re, const Mpf<P>& im, double* r2_out = nullptr) {
+  const double a = mpf_get_d(re), b = mpf_get_d(im);
+#if defined(__CUDA_ARCH__)
+  const double r2 = __dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b));
+#else
+  volatile double aa = a * a, bb = b * b;
+  const double r2 = aa + bb;
+#endif
+  if (r2_out) *r2_out = r2;
+  return r2 > 1024.0 * 1024.0;
+}
+
+// inCardioid (mandelbrot.cpp:63-71) in the view's precision: fourth and one
+// are 0.25 and 1.0.
+template <int P>
+MPF_HD bool mpf_in_cardioid(const Mpf<P>& zr, const Mpf<P>& zi) {
+  const Mpf<P> fourth = mpf_from_double<P>(0.25), one = mpf_from_double<P>(1.0);
+  const Mpf<P> xmf = mpf_sub(zr, fourth);
+  const Mpf<P> y2 = mpf_mul(zi, zi);
+  const Mpf<P> q = mpf_add(mpf_mul(xmf, xmf), y2);
+  const Mpf<P> lhs = mpf_mul(q, mpf_add(q, xmf));
+  const Mpf<P> rhs = mpf_mul(fourth, y2);
+  if (mpf_cmp(lhs, rhs) < 0) return true;
+  const Mpf<P> q2 = mpf_add(zr, one);
+  const Mpf<P> lhs2 = mpf_add(mpf_mul(q2, q2), y2);
+  return mpf_cmp(lhs2, mpf_mul(fourth, fourth)) < 0;
+}
+
+}  // namespace nmg

@@ -273,6 +273,29 @@ void MPView::coordinates(std::vector<D2>& re, std::vector<D2>& im) const {
   }
 }
 
+void mp_record(mpf_srcptr x, int limbs, uint64_t* out) {
+  const int size = x->_mp_size;
+  const int n = size < 0 ? -size : size;
+  const int32_t s = size < 0 ? -1 : (size > 0 ? 1 : 0);
+  out[0] = ((uint64_t)(uint32_t)(int32_t)(s ? x->_mp_exp : 0) << 32) | (uint32_t)s;
+  for (int i = 0; i < limbs; i++) out[1 + i] = i < n ? x->_mp_d[n - 1 - i] : 0;
+}
+
+void MPView::coordinates_mp(std::vector<uint64_t>& re, std::vector<uint64_t>& im) const {
+  const int limbs = mp_limbs_for_bits(bits_), w = mp_record_words(limbs);
+  re.assign((size_t)nc_ * w, 0);
+  im.assign((size_t)nr_ * w, 0);
+  Mpf p(bits_), t(bits_);
+  for (int c = 0; c < nc_; c++) {
+    coord_re(c, p, t);
+    mp_record(p.p(), limbs, &re[(size_t)c * w]);
+  }
+  for (int r = 0; r < nr_; r++) {
+    coord_im(r, p, t);
+    mp_record(p.p(), limbs, &im[(size_t)r * w]);
+  }
+}
+
 void MPView::eps_tables(const OrbitData&, std::vector<double>& er, std::vector<double>& ei) const {
   // Y.re = Y0.re - X[0].re; eps.re = Y.re.get_d()   (mandelbrot.cpp:155-159)
   er.resize(nc_);
@@ -328,8 +351,10 @@ static bool rfe_less_host(RFE x, RFE y) {
   return std::scalbn(x.m, x.e - ex) < std::scalbn(y.m, y.e - ey);
 }
 
-int MPView::precompute(int threads, OrbitData& od, int reference_mode) {
+int MPView::precompute(int threads, OrbitData& od, int reference_mode, bool keep_mp) {
   od = OrbitData();
+  const int mp_limbs = mp_limbs_for_bits(bits_), mp_w = mp_record_words(mp_limbs);
+  if (keep_mp) od.mp_limbs = mp_limbs;
   // Probe points of findProbe (mandelbrot.cpp:77-83), in the reference's order,
   // or the view center alone: pointAt(nr/2 - 1, nc/2) is exactly the center.
   std::vector<std::pair<int, int>> pts;
@@ -407,6 +432,12 @@ int MPView::precompute(int threads, OrbitData& od, int reference_mode) {
     od.xhi.push_back(hi);
     od.xlo.push_back(lo);
     od.z.push_back(hi);
+    if (keep_mp) {
+      const size_t at = od.xmp.size();
+      od.xmp.resize(at + 2 * (size_t)mp_w);
+      mp_record(xr.p(), mp_limbs, &od.xmp[at]);
+      mp_record(xi.p(), mp_limbs, &od.xmp[at + mp_w]);
+    }
     od.a.push_back({ar.d(), ai.d()});
     od.b.push_back({br.d(), bi.d()});
     od.c.push_back({c_r.d(), c_i.d()});

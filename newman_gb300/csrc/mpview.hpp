@@ -66,7 +66,20 @@ struct OrbitData {
   // The orbit alone, for the FE32 path on a view the reference renders with
   // its double loop (no series: those samples start at iteration 0).
   bool double_loop = false;
+  // The orbit X[0..xlen) in the view's arbitrary precision, for the
+  // reference-exact path (filled when precompute is asked for it): per
+  // element the records of re and im, each mp_record_words(limbs) words.
+  int mp_limbs = 0;
+  std::vector<uint64_t> xmp;
 };
+
+// One arbitrary-precision value as device words: word 0 holds the limb
+// exponent (high 32 bits) and the sign (low 32 bits, -1, 0 or 1), then
+// `limbs` limbs, most significant first, zero below the value's own.
+inline int mp_record_words(int limbs) { return limbs + 1; }
+// Limbs a value of the view's precision holds: GMP's P + 1 for mpf_init2(bits).
+inline int mp_limbs_for_bits(unsigned long bits) { return (int)((bits + 127) / 64) + 1; }
+void mp_record(mpf_srcptr x, int limbs, uint64_t* out);
 
 // Where the reference orbit starts.
 enum ReferenceMode {
@@ -117,7 +130,12 @@ class MPView {
 
   // findProbe + computeSeries (mandelbrot.cpp:73-131), probes on `threads`
   // host threads (or the view center only, REFERENCE_CENTER).  Fills `out`.
-  int precompute(int threads, OrbitData& out, int reference_mode = REFERENCE_PROBES);
+  int precompute(int threads, OrbitData& out, int reference_mode = REFERENCE_PROBES,
+                 bool keep_mp = false);
+  // computeRow's pt.re per column and pt.im per row (mandelbrot.cpp:271,275)
+  // as arbitrary-precision records (mp_record) of mp_limbs_for_bits(bits())
+  // limbs.
+  void coordinates_mp(std::vector<uint64_t>& re, std::vector<uint64_t>& im) const;
 
   // For the FE32 path on a double-loop view: the orbit of the view center at
   // `orbit_bits` of precision (no series), and per column / row the exact

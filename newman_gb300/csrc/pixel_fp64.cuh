@@ -206,16 +206,8 @@ NM_HD bool above_bits(double r2, double bailout2) {
 #endif
 }
 
-// Returns true when the sample is already decided (cardioid).
-NM_HD bool hw_init(const DeviceView& v, int r, int c, HwState& st, EscapeValue& out, double& sm,
-                   bool& undecided) {
-  const Dbl2 px = v.coord_re[c], py = v.coord_im[r];
-  undecided = false;
-  if (v.cardioid_mode == CARDIOID_PER_SAMPLE && in_cardioid_dd(px, py, undecided)) {
-    out = {v.N, 0.0f};
-    sm = 0.0;
-    return true;
-  }
+// The double loop's start at Z0 = descend(pt) (mandelbrot.cpp:234, 242).
+NM_HD void hw_start(Dbl2 px, Dbl2 py, HwState& st) {
   st.z0r = px.x;
   st.z0i = py.x;
   st.zr = px.x;
@@ -226,6 +218,19 @@ NM_HD bool hw_init(const DeviceView& v, int r, int c, HwState& st, EscapeValue& 
   st.ci = py.x;
   st.it = 0;
   st.save_at = 1;
+}
+
+// Returns true when the sample is already decided (cardioid).
+NM_HD bool hw_init(const DeviceView& v, int r, int c, HwState& st, EscapeValue& out, double& sm,
+                   bool& undecided) {
+  const Dbl2 px = v.coord_re[c], py = v.coord_im[r];
+  undecided = false;
+  if (v.cardioid_mode == CARDIOID_PER_SAMPLE && in_cardioid_dd(px, py, undecided)) {
+    out = {v.N, 0.0f};
+    sm = 0.0;
+    return true;
+  }
+  hw_start(px, py, st);
   return false;
 }
 

@@ -64,6 +64,7 @@ int persistent_blocks(KernelKind kind, int device) {
 cudaError_t launch_render(KernelKind kind, const DeviceView& v, const RenderCtl& ctl,
                           cudaStream_t stream, int blocks, int chunk) {
   if (kind == KERNEL_FE32) return launch_fe32(v, ctl, stream, blocks, chunk);
+  if (kind == KERNEL_MP || kind == KERNEL_HW_MP) return launch_mp(kind, v, ctl, stream, blocks, chunk);
   note_launches(1);
   if (kind == KERNEL_HW)
     hw_kernel<<<blocks, kPersistentThreads, 0, stream>>>(v, ctl, chunk);

@@ -116,6 +116,13 @@ struct DeviceView {
   const CFFE* sa_c32;
   const TFE* sa_min32;     // [xlen]
 
+  // the reference-exact path: values in the view's arbitrary precision as
+  // records of mp_limbs limbs (mpf_fixed.cuh; word 0: exponent << 32 | sign)
+  int32_t mp_limbs;        // limbs of a value (GMP's P + 1)
+  const uint64_t* coord_re_mp;  // [nc] pt.re
+  const uint64_t* coord_im_mp;  // [nr] pt.im
+  const uint64_t* x_mp;         // [xlen] X[k].re, X[k].im
+
   EscapeValue* grid;       // [nr*nc]
   double* smooth64;        // optional [nr*nc] unrounded smoothing
 

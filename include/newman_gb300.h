@@ -140,6 +140,12 @@ int nm_precompute(nm_handle* h);
 /* Re-issue the host-to-device copy of the precomputed tables on the handle's
    stream (asynchronous). */
 int nm_upload(nm_handle* h);
+/* No reference counterpart (the reference keeps X, A, B, C private,
+   mandelbrot.h:45-50): the last precompute's orbit and series as doubles,
+   get_d of each (mandelbrot.cpp:166-168), n = X.size() entries of (re, im)
+   pairs in each non-null array; xlo holds get_d(X - get_d(X)).  n must be
+   NM_STAT_ORBIT_LENGTH. */
+int nm_get_orbit(nm_handle* h, double* x, double* xlo, double* a, double* b, double* c, int n);
 
 /* computeRow(r), mandelbrot.cpp:269-283: render one row, synchronously. */
 int nm_compute_row(nm_handle* h, int r);

@@ -37,7 +37,7 @@ EXPORTS = (
     "nm_create", "nm_copy", "nm_destroy", "nm_last_error", "nm_set_view", "nm_get_view",
     "nm_set_iterations", "nm_get_iterations", "nm_set_tolerance", "nm_rows", "nm_cols",
     "nm_use_hardware", "nm_set_path", "nm_set_option", "nm_get_stat", "nm_precompute",
-    "nm_upload", "nm_compute_row", "nm_render_rows", "nm_render", "nm_synchronize", "nm_cancel",
+    "nm_upload", "nm_get_orbit", "nm_compute_row", "nm_render_rows", "nm_render", "nm_synchronize", "nm_cancel",
     "nm_at", "nm_at_sc", "nm_scale_up", "nm_scale_down", "nm_reduce", "nm_get_grid",
     "nm_get_smoothing64", "nm_device_grid", "nm_point_at", "nm_translate", "nm_zoom",
     "nm_zoom_at", "nm_load_legacy", "nm_save", "nm_peak_flops", "nm_render_fe32_noalloc",
@@ -94,6 +94,7 @@ def load_library(path=LIB_PATH):
         "nm_get_stat": (i32, [vp, i32, P(ll)]),
         "nm_precompute": (i32, [vp]),
         "nm_upload": (i32, [vp]),
+        "nm_get_orbit": (i32, [vp, vp, vp, vp, vp, vp, i32]),
         "nm_compute_row": (i32, [vp, i32]),
         "nm_render_rows": (i32, [vp, i32, i32, vp]),
         "nm_render": (i32, [vp]),
@@ -448,6 +449,14 @@ class Mandelbrot:
 
     def upload(self):
         _check(_lib.nm_upload(self._h))
+
+    def orbit(self):
+        """(X, X - get_d(X), A, B, C) of the last precompute as (n, 2) double
+        arrays of get_d values."""
+        n = self.stat(STAT_ORBIT_LENGTH)
+        out = [np.empty((n, 2), np.float64) for _ in range(5)]
+        _check(_lib.nm_get_orbit(self._h, *[o.ctypes.data for o in out], n))
+        return tuple(out)
 
     def computeRow(self, r):
         _check(_lib.nm_compute_row(self._h, int(r)))

@@ -596,6 +596,33 @@ int nm_get_stat(nm_handle* h, int stat, long long* value) {
   return fail(NM_ERR_ARG, "unknown stat %d", stat);
 }
 
+// findProbe's orbit lengths on the handle's GPU (the same arithmetic as the
+// host's, bit for bit); false when no GPU is at hand or the precision has no
+// kernel, and the host threads find them.
+static bool gpu_probe_lengths(void* ctx, int limbs, const std::vector<uint64_t>& re,
+                              const std::vector<uint64_t>& im, int N, std::vector<int>& len) {
+  nm_handle* h = static_cast<nm_handle*>(ctx);
+  if (limbs < nmg::kMpMinLimbs || limbs > nmg::kMpMaxLimbs) return false;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+    cudaGetLastError();
+    return false;
+  }
+  if (ensure_device(h) != NM_OK) return false;
+  const int n = (int)len.size();
+  DevBuf<uint64_t> d_re, d_im;
+  DevBuf<int32_t> d_len;
+  if (d_re.reserve(re.size()) || d_im.reserve(im.size()) || d_len.reserve((size_t)n)) return false;
+  cudaStream_t s = h->stream;
+  if (cudaMemcpyAsync(d_re.p, re.data(), re.size() * 8, cudaMemcpyHostToDevice, s) ||
+      cudaMemcpyAsync(d_im.p, im.data(), im.size() * 8, cudaMemcpyHostToDevice, s) ||
+      nmg::launch_probes(limbs, d_re.p, d_im.p, n, N, d_len.p, s) ||
+      cudaMemcpyAsync(len.data(), d_len.p, (size_t)n * 4, cudaMemcpyDeviceToHost, s) ||
+      cudaStreamSynchronize(s))
+    return false;
+  return true;
+}
+
 int nm_precompute(nm_handle* h) {
   if (int rc = check_handle(h)) return rc;
   auto t0 = std::chrono::steady_clock::now();
@@ -617,7 +644,8 @@ int nm_precompute(nm_handle* h) {
   } else if (!h->view.use_hardware() ||
              (h->path != NM_PATH_REFERENCE && h->path != NM_PATH_MP)) {
     int threads = h->threads > 0 ? h->threads : (int)std::thread::hardware_concurrency();
-    if (h->view.precompute(threads, h->od, h->reference_mode, h->path == NM_PATH_MP))
+    if (h->view.precompute(threads, h->od, h->reference_mode, h->path == NM_PATH_MP,
+                           gpu_probe_lengths, h))
       return fail(NM_ERR_STATE, "precompute failed");
     h->view.eps_tables(h->od, h->eps_re, h->eps_im);
     if (!h->od.sa_fp64_ok) h->view.eps_tables_fe(h->eps_re_fe, h->eps_im_fe);
@@ -628,6 +656,20 @@ int nm_precompute(nm_handle* h) {
       std::chrono::duration<double, std::micro>(std::chrono::steady_clock::now() - t0).count();
   h->uploaded = false;  // copied to the GPU by nm_upload or the next render
   h->generation++;
+  return NM_OK;
+}
+
+int nm_get_orbit(nm_handle* h, double* x, double* xlo, double* a, double* b, double* c, int n) {
+  if (int rc = check_handle(h)) return rc;
+  if (!h->precomputed || h->od.double_loop) return fail(NM_ERR_STATE, "no precomputed orbit and series");
+  if (n != h->od.xlen) return fail(NM_ERR_ARG, "%d entries for an orbit of %d", n, h->od.xlen);
+  for (int i = 0; i < n; i++) {
+    if (x) x[2 * i] = h->od.xhi[i].x, x[2 * i + 1] = h->od.xhi[i].y;
+    if (xlo) xlo[2 * i] = h->od.xlo[i].x, xlo[2 * i + 1] = h->od.xlo[i].y;
+    if (a) a[2 * i] = h->od.a[i].x, a[2 * i + 1] = h->od.a[i].y;
+    if (b) b[2 * i] = h->od.b[i].x, b[2 * i + 1] = h->od.b[i].y;
+    if (c) c[2 * i] = h->od.c[i].x, c[2 * i + 1] = h->od.c[i].y;
+  }
   return NM_OK;
 }
 

@@ -54,6 +54,10 @@ enum KernelKind {
 constexpr int kMpMinLimbs = 3, kMpMaxLimbs = 9;
 cudaError_t launch_mp(KernelKind kind, const DeviceView& v, const RenderCtl& ctl,
                       cudaStream_t stream, int blocks, int chunk);
+// findProbe's orbit lengths on the GPU: n probe points as arbitrary-precision
+// records of `limbs` limbs (re[k], im[k]), lengths to len[k] (device memory).
+cudaError_t launch_probes(int limbs, const uint64_t* re, const uint64_t* im, int n, int N,
+                          int32_t* len, cudaStream_t stream);
 
 // Buffers of the FE32 pass pipeline (render_fe32.cu), one record per sample
 // index in tile order.

@@ -21,7 +21,9 @@
 //              difference of 1 followed by limb pairs (0, 2^64 - 1), which
 //              cancel to a 1 one limb lower -- and both operands are cut
 //              P + 1 limbs below the position so reached; exact difference;
-//   get_d(x)   x truncated toward zero to a double;
+//   get_d(x)   x truncated toward zero to a double (into the subnormal
+//              range too; +0 when nothing is left, of either sign; infinity
+//              beyond the double range);
 //   set_d(x)   exact.
 //
 // A value is sign, limb exponent e and the D = P + 1 limbs d[0..P], most
@@ -42,7 +44,7 @@
 namespace nmg {
 
 template <int P>
-struct Mpf {
+struct Mpfx {
   static_assert(P >= 2, "GMP's smallest mpf precision is 2 limbs (64 bits)");
   static constexpr int D = P + 1;
   uint64_t d[D];
@@ -102,36 +104,36 @@ MPF_HD uint64_t limb_at(const uint64_t (&d)[D], int k) {
 }  // namespace mpf_detail
 
 template <int P>
-MPF_HD Mpf<P> mpf_zero() {
-  Mpf<P> r;
+MPF_HD Mpfx<P> mpf_zero() {
+  Mpfx<P> r;
 #pragma unroll
-  for (int i = 0; i < Mpf<P>::D; i++) r.d[i] = 0;
+  for (int i = 0; i < Mpfx<P>::D; i++) r.d[i] = 0;
   r.e = 0;
   r.s = 0;
   return r;
 }
 
 template <int P>
-MPF_HD Mpf<P> mpf_neg(Mpf<P> a) {
+MPF_HD Mpfx<P> mpf_neg(Mpfx<P> a) {
   a.s = -a.s;
   return a;
 }
 
 // -1, 0, 1 as |a| is below, equal to or above |b|.
 template <int P>
-MPF_HD int mpf_cmp_abs(const Mpf<P>& a, const Mpf<P>& b) {
+MPF_HD int mpf_cmp_abs(const Mpfx<P>& a, const Mpfx<P>& b) {
   if (a.s == 0 || b.s == 0) return (a.s != 0) - (b.s != 0);
   if (a.e != b.e) return a.e < b.e ? -1 : 1;
   int r = 0;
 #pragma unroll
-  for (int i = 0; i < Mpf<P>::D; i++)
+  for (int i = 0; i < Mpfx<P>::D; i++)
     if (r == 0 && a.d[i] != b.d[i]) r = a.d[i] < b.d[i] ? -1 : 1;
   return r;
 }
 
 // mpf_cmp: -1, 0, 1 as a is below, equal to or above b.
 template <int P>
-MPF_HD int mpf_cmp(const Mpf<P>& a, const Mpf<P>& b) {
+MPF_HD int mpf_cmp(const Mpfx<P>& a, const Mpfx<P>& b) {
   if (a.s != b.s) return a.s < b.s ? -1 : 1;
   const int m = mpf_cmp_abs(a, b);
   return a.s < 0 ? -m : m;
@@ -139,7 +141,7 @@ MPF_HD int mpf_cmp(const Mpf<P>& a, const Mpf<P>& b) {
 
 // mpf_mul into a destination of P limbs of precision.
 template <int P>
-MPF_HD Mpf<P> mpf_mul(const Mpf<P>& a, const Mpf<P>& b) {
+MPF_HD Mpfx<P> mpf_mul(const Mpfx<P>& a, const Mpfx<P>& b) {
   using namespace mpf_detail;
   constexpr int D = P + 1;
   if (a.s == 0 || b.s == 0) return mpf_zero<P>();
@@ -168,7 +170,7 @@ MPF_HD Mpf<P> mpf_mul(const Mpf<P>& a, const Mpf<P>& b) {
   }
   // top limb zero: one limb lower
   const bool adj = r[2 * P - 1] == 0;
-  Mpf<P> o;
+  Mpfx<P> o;
 #pragma unroll
   for (int k = 0; k < D; k++) {
     const uint64_t hi = r[2 * P - 1 - k];
@@ -182,10 +184,10 @@ MPF_HD Mpf<P> mpf_mul(const Mpf<P>& a, const Mpf<P>& b) {
 
 // mpf_mul(r, two, a) with two = 2.0: 2 times the top P limbs of a, exactly.
 template <int P>
-MPF_HD Mpf<P> mpf_mul2(const Mpf<P>& a) {
+MPF_HD Mpfx<P> mpf_mul2(const Mpfx<P>& a) {
   constexpr int D = P + 1;
   if (a.s == 0) return a;
-  Mpf<P> o;
+  Mpfx<P> o;
   const uint64_t top = a.d[0] >> 63;
   if (top) {  // the product gains a limb
     o.d[0] = 1;
@@ -206,17 +208,17 @@ MPF_HD Mpf<P> mpf_mul2(const Mpf<P>& a) {
 
 // mpf_add (and mpf_sub = mpf_add with -b) into a destination of P limbs.
 template <int P>
-MPF_HD Mpf<P> mpf_add(const Mpf<P>& a, const Mpf<P>& b) {
+MPF_HD Mpfx<P> mpf_add(const Mpfx<P>& a, const Mpfx<P>& b) {
   using namespace mpf_detail;
   constexpr int D = P + 1;
   if (a.s == 0) return b;
   if (b.s == 0) return a;
-  Mpf<P> o;
+  Mpfx<P> o;
   if (a.s == b.s) {
     // both cut at limb position E - P: the top P limbs below E
     const bool a_hi = a.e >= b.e;
-    const Mpf<P>& u = a_hi ? a : b;
-    const Mpf<P>& v = a_hi ? b : a;
+    const Mpfx<P>& u = a_hi ? a : b;
+    const Mpfx<P>& v = a_hi ? b : a;
     const int off = u.e - v.e;  // v's limb k sits at u's index k + off
     uint64_t sum[P];
     uint64_t c = 0;
@@ -239,8 +241,8 @@ MPF_HD Mpf<P> mpf_add(const Mpf<P>& a, const Mpf<P>& b) {
   // opposite signs: U the larger magnitude
   const int m = mpf_cmp_abs(a, b);
   if (m == 0) return mpf_zero<P>();
-  const Mpf<P>& U = m > 0 ? a : b;
-  const Mpf<P>& W = m > 0 ? b : a;
+  const Mpfx<P>& U = m > 0 ? a : b;
+  const Mpfx<P>& W = m > 0 ? b : a;
   const int off = U.e - W.e;  // W's limb k sits at U's index k + off; off >= 0
   // first index where the limbs differ (equal exponents: equal leading limbs
   // cancel)
@@ -293,45 +295,58 @@ MPF_HD Mpf<P> mpf_add(const Mpf<P>& a, const Mpf<P>& b) {
 }
 
 template <int P>
-MPF_HD Mpf<P> mpf_sub(const Mpf<P>& a, const Mpf<P>& b) {
+MPF_HD Mpfx<P> mpf_sub(const Mpfx<P>& a, const Mpfx<P>& b) {
   return mpf_add(a, mpf_neg(b));
 }
 
-// mpf_get_d: truncation toward zero (values in the normal double range).
+// mpf_get_d: truncation toward zero.
 template <int P>
-MPF_HD double mpf_get_d(const Mpf<P>& a) {
+MPF_HD double mpf_get_d(const Mpfx<P>& a) {
   using namespace mpf_detail;
   if (a.s == 0) return 0.0;
   const int lz = clz64(a.d[0]);
-  uint64_t m = a.d[0] << lz;
+  uint64_t m = a.d[0] << lz;  // the top 64 bits, leading bit set
   if (lz) m |= a.d[1] >> (64 - lz);
-  m >>= 11;  // the top 53 bits
-  const int e2 = 64 * (a.e - 1) + (63 - lz) - 52;  // value = m * 2^e2
-  // m * 2^e2 with m < 2^53: exact while the result is a normal double
-  double x = (double)m;
-  int k = e2;
-  // scale by powers of two in steps that stay exact
-  while (k > 900) {
-    x *= 0x1p900;
-    k -= 900;
-  }
-  while (k < -900) {
-    x *= 0x1p-900;
-    k += 900;
-  }
+  const long top = 64L * (a.e - 1) + (63 - lz);  // weight 2^top of the leading bit
   union {
     double f;
     uint64_t u;
-  } sc;
-  sc.u = (uint64_t)(k + 1023) << 52;
-  x *= sc.f;
+  } r;
+  if (top > 1023) {
+    r.u = 0x7ff0000000000000ull;  // infinity
+  } else if (top >= -1022) {      // normal: the top 53 bits
+    r.u = ((uint64_t)(top + 1023) << 52) | ((m >> 11) & ((1ull << 52) - 1));
+  } else {                        // subnormal: multiples of 2^-1074, truncated
+    const long sh = -1074 - (top - 63);
+    r.u = sh >= 64 ? 0 : m >> sh;
+    if (r.u == 0) return 0.0;
+  }
+  if (a.s < 0) r.u |= 1ull << 63;
+  return r.f;
+}
+
+// mpf_get_d_2exp: the value as m * 2^exp with 0.5 <= |m| < 1, m truncated
+// toward zero to 53 bits (m = 0, exp = 0 for zero).
+template <int P>
+MPF_HD double mpf_get_d_2exp(long* exp, const Mpfx<P>& a) {
+  using namespace mpf_detail;
+  if (a.s == 0) {
+    *exp = 0;
+    return 0.0;
+  }
+  const int lz = clz64(a.d[0]);
+  uint64_t m = a.d[0] << lz;
+  if (lz) m |= a.d[1] >> (64 - lz);
+  m >>= 11;
+  *exp = 64L * a.e - lz;
+  const double x = (double)m * 0x1p-53;
   return a.s < 0 ? -x : x;
 }
 
 // mpf_set_d: a finite double exactly.
 template <int P>
-MPF_HD Mpf<P> mpf_from_double(double x) {
-  Mpf<P> o = mpf_zero<P>();
+MPF_HD Mpfx<P> mpf_from_double(double x) {
+  Mpfx<P> o = mpf_zero<P>();
   if (x == 0.0) return o;
   union {
     double f;
@@ -366,10 +381,10 @@ MPF_HD Mpf<P> mpf_from_double(double x) {
 // computeOrbit / getIterations (mandelbrot.cpp:102-103, :213-214):
 //   re = X.re * X.re - X.im * X.im + X0.re;   im = 2.0 * (X.re * X.im) + X0.im
 template <int P>
-MPF_HD void mpf_orbit_step(const Mpf<P>& xr, const Mpf<P>& xi, const Mpf<P>& x0r,
-                           const Mpf<P>& x0i, Mpf<P>& nr, Mpf<P>& ni) {
-  const Mpf<P> t1 = mpf_sub(mpf_mul(xr, xr), mpf_mul(xi, xi));
-  const Mpf<P> t3 = mpf_mul2(mpf_mul(xr, xi));
+MPF_HD void mpf_orbit_step(const Mpfx<P>& xr, const Mpfx<P>& xi, const Mpfx<P>& x0r,
+                           const Mpfx<P>& x0i, Mpfx<P>& nr, Mpfx<P>& ni) {
+  const Mpfx<P> t1 = mpf_sub(mpf_mul(xr, xr), mpf_mul(xi, xi));
+  const Mpfx<P> t3 = mpf_mul2(mpf_mul(xr, xi));
   nr = mpf_add(t1, x0r);
   ni = mpf_add(t3, x0i);
 }
@@ -377,7 +392,7 @@ MPF_HD void mpf_orbit_step(const Mpf<P>& xr, const Mpf<P>& xi, const Mpf<P>& x0r
 // bailedOut (mandelbrot.cpp:58-61): sqMag(descend(z)) > 1024^2 in doubles,
 // unfused.
 template <int P>
-MPF_HD bool mpf_bailed_out(const Mpf<P>& re, const Mpf<P>& im, double* r2_out = nullptr) {
+MPF_HD bool mpf_bailed_out(const Mpfx<P>& re, const Mpfx<P>& im, double* r2_out = nullptr) {
   const double a = mpf_get_d(re), b = mpf_get_d(im);
 #if defined(__CUDA_ARCH__)
   const double r2 = __dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b));
@@ -392,16 +407,16 @@ MPF_HD bool mpf_bailed_out(const Mpf<P>& re, const Mpf<P>& im, double* r2_out = 
 // inCardioid (mandelbrot.cpp:63-71) in the view's precision: fourth and one
 // are 0.25 and 1.0.
 template <int P>
-MPF_HD bool mpf_in_cardioid(const Mpf<P>& zr, const Mpf<P>& zi) {
-  const Mpf<P> fourth = mpf_from_double<P>(0.25), one = mpf_from_double<P>(1.0);
-  const Mpf<P> xmf = mpf_sub(zr, fourth);
-  const Mpf<P> y2 = mpf_mul(zi, zi);
-  const Mpf<P> q = mpf_add(mpf_mul(xmf, xmf), y2);
-  const Mpf<P> lhs = mpf_mul(q, mpf_add(q, xmf));
-  const Mpf<P> rhs = mpf_mul(fourth, y2);
+MPF_HD bool mpf_in_cardioid(const Mpfx<P>& zr, const Mpfx<P>& zi) {
+  const Mpfx<P> fourth = mpf_from_double<P>(0.25), one = mpf_from_double<P>(1.0);
+  const Mpfx<P> xmf = mpf_sub(zr, fourth);
+  const Mpfx<P> y2 = mpf_mul(zi, zi);
+  const Mpfx<P> q = mpf_add(mpf_mul(xmf, xmf), y2);
+  const Mpfx<P> lhs = mpf_mul(q, mpf_add(q, xmf));
+  const Mpfx<P> rhs = mpf_mul(fourth, y2);
   if (mpf_cmp(lhs, rhs) < 0) return true;
-  const Mpf<P> q2 = mpf_add(zr, one);
-  const Mpf<P> lhs2 = mpf_add(mpf_mul(q2, q2), y2);
+  const Mpfx<P> q2 = mpf_add(zr, one);
+  const Mpfx<P> lhs2 = mpf_add(mpf_mul(q2, q2), y2);
   return mpf_cmp(lhs2, mpf_mul(fourth, fourth)) < 0;
 }
 

@@ -7,6 +7,8 @@
 // expressions, so the exported doubles are the values the reference reads.
 #include "mpview.hpp"
 
+#include "mpf_fixed.cuh"
+
 #include <algorithm>
 #include <atomic>
 #include <cmath>
@@ -60,6 +62,153 @@ int orbit_length(mpf_srcptr cr, mpf_srcptr ci, int N, unsigned long bits) {
     ai.swap(bi);
   }
   return N;
+}
+
+// ---- the same arithmetic on fixed-precision limbs (mpf_fixed.cuh) -----------
+// GMP's results bit for bit without a library call per operation: the probe
+// search, the winner's orbit and its series run here for precisions of
+// kFixedMinP .. kFixedMaxP limbs (64 .. 1216 bits).
+constexpr int kFixedMinP = 2, kFixedMaxP = 20;
+
+template <int P>
+Mpfx<P> fixed_of(mpf_srcptr x) {
+  Mpfx<P> r = mpf_zero<P>();
+  const int size = x->_mp_size;
+  const int n = size < 0 ? -size : size;
+  if (n == 0) return r;
+  for (int i = 0; i < Mpfx<P>::D && i < n; i++) r.d[i] = x->_mp_d[n - 1 - i];
+  r.e = (int32_t)x->_mp_exp;
+  r.s = size < 0 ? -1 : 1;
+  return r;
+}
+
+template <int P>
+void record_of(const Mpfx<P>& x, uint64_t* out) {
+  out[0] = ((uint64_t)(uint32_t)(x.s ? x.e : 0) << 32) | (uint32_t)x.s;
+  for (int i = 0; i < Mpfx<P>::D; i++) out[1 + i] = x.d[i];
+}
+
+template <int P>
+int fixed_orbit_length(const Mpfx<P>& cr, const Mpfx<P>& ci, int N) {
+  Mpfx<P> xr = cr, xi = ci;
+  for (int i = 1; i < N; i++) {
+    Mpfx<P> nr, ni;
+    mpf_orbit_step(xr, xi, cr, ci, nr, ni);
+    if (mpf_bailed_out(nr, ni)) return i;
+    xr = nr;
+    xi = ni;
+  }
+  return N;
+}
+
+// get_d of a complex value as floatexp with one exponent (cfe_of below).
+template <int P>
+CFE fixed_cfe(const Mpfx<P>& re, const Mpfx<P>& im) {
+  long er = 0, ei = 0;
+  const double dr = mpf_get_d_2exp(&er, re), di = mpf_get_d_2exp(&ei, im);
+  if (dr == 0.0 && di == 0.0) return {0.0, 0.0, 0};
+  const long e = dr == 0.0 ? ei : di == 0.0 ? er : std::max(er, ei);
+  return {std::ldexp(dr, (int)(er - e)), std::ldexp(di, (int)(ei - e)), (int32_t)e};
+}
+
+// The winner's orbit X and series A, B, C (mandelbrot.cpp:97-131) in one pass,
+// exported as MPView::precompute's GMP loop exports them.  Returns true when
+// the orbit escaped (its escaped element then ends od.z).
+template <int P>
+bool fixed_orbit_series(mpf_srcptr cr_g, mpf_srcptr ci_g, int N, OrbitData& od, bool keep_mp) {
+  const Mpfx<P> cr = fixed_of<P>(cr_g), ci = fixed_of<P>(ci_g);
+  const Mpfx<P> one = mpf_from_double<P>(1.0);
+  Mpfx<P> xr = cr, xi = ci;
+  Mpfx<P> ar = one, ai = mpf_zero<P>(), br = mpf_zero<P>(), bi = mpf_zero<P>();
+  Mpfx<P> c_r = mpf_zero<P>(), c_i = mpf_zero<P>();
+  const int w = mp_record_words(Mpfx<P>::D);
+  auto split = [](const Mpfx<P>& v, double& hi, double& lo) {
+    hi = mpf_get_d(v);
+    lo = mpf_get_d(mpf_sub(v, mpf_from_double<P>(hi)));
+  };
+  Mpfx<P> nxr, nxi;
+  for (int i = 0;; i++) {
+    D2 hi, lo;
+    split(xr, hi.x, lo.x);
+    split(xi, hi.y, lo.y);
+    od.xhi.push_back(hi);
+    od.xlo.push_back(lo);
+    od.z.push_back(hi);
+    if (keep_mp) {
+      const size_t at = od.xmp.size();
+      od.xmp.resize(at + 2 * (size_t)w);
+      record_of(xr, &od.xmp[at]);
+      record_of(xi, &od.xmp[at + w]);
+    }
+    od.a.push_back({mpf_get_d(ar), mpf_get_d(ai)});
+    od.b.push_back({mpf_get_d(br), mpf_get_d(bi)});
+    od.c.push_back({mpf_get_d(c_r), mpf_get_d(c_i)});
+    od.a_fe.push_back(fixed_cfe(ar, ai));
+    od.b_fe.push_back(fixed_cfe(br, bi));
+    od.c_fe.push_back(fixed_cfe(c_r, c_i));
+    if (i + 1 >= N) return false;  // X.resize(N) is full
+    mpf_orbit_step(xr, xi, cr, ci, nxr, nxi);
+    if (mpf_bailed_out(nxr, nxi)) {
+      od.z.push_back({mpf_get_d(nxr), mpf_get_d(nxi)});  // the element that escaped
+      return true;
+    }
+    // A, B, C at i + 1 from X[i] in the reference's grouping (:122-129)
+    const Mpfx<P> nar = mpf_add(mpf_mul2(mpf_sub(mpf_mul(xr, ar), mpf_mul(xi, ai))), one);
+    const Mpfx<P> nai = mpf_mul2(mpf_add(mpf_mul(xr, ai), mpf_mul(xi, ar)));
+    const Mpfx<P> nbr = mpf_sub(
+        mpf_add(mpf_mul2(mpf_sub(mpf_mul(xr, br), mpf_mul(xi, bi))), mpf_mul(nar, nar)),
+        mpf_mul(nai, nai));
+    const Mpfx<P> nbi = mpf_mul2(
+        mpf_add(mpf_add(mpf_mul(xr, bi), mpf_mul(xi, br)), mpf_mul(nar, nai)));
+    const Mpfx<P> ncr = mpf_mul2(mpf_sub(
+        mpf_add(mpf_sub(mpf_mul(xr, c_r), mpf_mul(xi, c_i)), mpf_mul(nar, nbr)),
+        mpf_mul(nai, nbi)));
+    const Mpfx<P> nci = mpf_mul2(mpf_add(
+        mpf_add(mpf_add(mpf_mul(xr, c_i), mpf_mul(xi, c_r)), mpf_mul(nar, nbi)),
+        mpf_mul(nai, nbr)));
+    ar = nar; ai = nai;
+    br = nbr; bi = nbi;
+    c_r = ncr; c_i = nci;
+    xr = nxr;
+    xi = nxi;
+  }
+}
+
+// Probe lengths and the winner's orbit and series at P limbs: probe k's
+// coordinates are (pr[k], pi[k]).
+template <int P>
+void fixed_probe_lengths(const std::vector<Mpf>& pr, const std::vector<Mpf>& pi, int N,
+                         int threads, std::vector<int>& len) {
+  std::atomic<size_t> next{0};
+  auto worker = [&]() {
+    for (;;) {
+      const size_t k = next.fetch_add(1);
+      if (k >= pr.size()) break;
+      len[k] = fixed_orbit_length(fixed_of<P>(pr[k].p()), fixed_of<P>(pi[k].p()), N);
+    }
+  };
+  const int T = std::max(1, std::min<int>(threads, (int)pr.size()));
+  std::vector<std::thread> pool;
+  for (int t = 1; t < T; t++) pool.emplace_back(worker);
+  worker();
+  for (auto& t : pool) t.join();
+}
+
+template <int P>
+bool fixed_dispatch(int p, const std::vector<Mpf>& pr, const std::vector<Mpf>& pi, int N,
+                    int threads, std::vector<int>& len, mpf_srcptr* winner, OrbitData* od,
+                    bool keep_mp, bool* escaped) {
+  if constexpr (P > kFixedMaxP) {
+    return false;
+  } else {
+    if (p != P)
+      return fixed_dispatch<P + 1>(p, pr, pi, N, threads, len, winner, od, keep_mp, escaped);
+    if (!winner)
+      fixed_probe_lengths<P>(pr, pi, N, threads, len);
+    else
+      *escaped = fixed_orbit_series<P>(winner[0], winner[1], N, *od, keep_mp);
+    return true;
+  }
 }
 
 // Interval arithmetic in double with outward slack, for the view-box
@@ -351,7 +500,8 @@ static bool rfe_less_host(RFE x, RFE y) {
   return std::scalbn(x.m, x.e - ex) < std::scalbn(y.m, y.e - ey);
 }
 
-int MPView::precompute(int threads, OrbitData& od, int reference_mode, bool keep_mp) {
+int MPView::precompute(int threads, OrbitData& od, int reference_mode, bool keep_mp,
+                       ProbeLengths probe_lengths, void* probe_ctx) {
   od = OrbitData();
   const int mp_limbs = mp_limbs_for_bits(bits_), mp_w = mp_record_words(mp_limbs);
   if (keep_mp) od.mp_limbs = mp_limbs;
@@ -370,7 +520,32 @@ int MPView::precompute(int threads, OrbitData& od, int reference_mode, bool keep
   }
 
   std::vector<int> len(pts.size(), N_);
-  if (pts.size() > 1) {
+  const int P = (int)((bits_ + 127) / 64);  // GMP's limbs of precision
+  const bool fixed = P >= kFixedMinP && P <= kFixedMaxP;
+  bool probed = false;
+  if (pts.size() > 1 && probe_lengths) {
+    const int limbs = mp_limbs_for_bits(bits_), w = mp_record_words(limbs);
+    std::vector<uint64_t> re(pts.size() * w), im(pts.size() * w);
+    Mpf p(bits_), tmp(bits_);
+    for (size_t k = 0; k < pts.size(); k++) {
+      coord_re(pts[k].second, p, tmp);
+      mp_record(p.p(), limbs, &re[k * w]);
+      coord_im(pts[k].first, p, tmp);
+      mp_record(p.p(), limbs, &im[k * w]);
+    }
+    probed = probe_lengths(probe_ctx, limbs, re, im, N_, len);
+  }
+  if (probed) {
+    // lengths from the GPU
+  } else if (pts.size() > 1 && fixed) {
+    std::vector<Mpf> pr(pts.size(), Mpf(bits_)), pi(pts.size(), Mpf(bits_));
+    Mpf tmp(bits_);
+    for (size_t k = 0; k < pts.size(); k++) {
+      coord_re(pts[k].second, pr[k], tmp);
+      coord_im(pts[k].first, pi[k], tmp);
+    }
+    fixed_dispatch<kFixedMinP>(P, pr, pi, N_, threads, len, nullptr, nullptr, false, nullptr);
+  } else if (pts.size() > 1) {
   std::atomic<size_t> next{0};
   auto worker = [&]() {
     Mpf pr(bits_), pi(bits_), tmp(bits_);
@@ -402,6 +577,17 @@ int MPView::precompute(int threads, OrbitData& od, int reference_mode, bool keep
   coord_im(pts[best].first, ci, tmp);
   x0re_ = cr;
   x0im_ = ci;
+  const size_t cap = (size_t)std::min(N_, 1 << 20) + 2;
+  od.z.reserve(cap);
+  od.z.push_back({0.0, 0.0});
+  if (fixed) {
+    mpf_srcptr winner[2] = {cr.p(), ci.p()};
+    bool escaped = false;
+    fixed_dispatch<kFixedMinP>(P, {}, {}, N_, threads, len, winner, &od, keep_mp, &escaped);
+    od.xlen = (int)od.xhi.size();
+    finish_thresholds(od);
+    return 0;
+  }
   StepTemps s(bits_);
   Mpf xr(bits_), xi(bits_), nxr(bits_), nxi(bits_);
   Mpf ar(bits_), ai(bits_), br(bits_), bi(bits_), c_r(bits_), c_i(bits_);
@@ -414,9 +600,6 @@ int MPView::precompute(int threads, OrbitData& od, int reference_mode, bool keep
   mpf_set_d(bi.p(), 0.0);
   mpf_set_d(c_r.p(), 0.0);
   mpf_set_d(c_i.p(), 0.0);
-  const size_t cap = (size_t)std::min(N_, 1 << 20) + 2;
-  od.z.reserve(cap);
-  od.z.push_back({0.0, 0.0});
   auto split = [&](mpf_srcptr v, double& hi, double& lo) {
     hi = mpf_get_d(v);
     mpf_set_d(h.p(), hi);
@@ -484,10 +667,14 @@ int MPView::precompute(int threads, OrbitData& od, int reference_mode, bool keep
     xr.swap(nxr);
     xi.swap(nxi);
   }
-  const int xlen = (int)od.xhi.size();
-  od.xlen = xlen;
+  od.xlen = (int)od.xhi.size();
   if (escaped) od.z.push_back({nxr.d(), nxi.d()});  // the element that escaped
+  finish_thresholds(od);
+  return 0;
+}
 
+void MPView::finish_thresholds(OrbitData& od) const {
+  const int xlen = od.xlen;
   // Series instability thresholds: term i fires when tol |b|^2 < |c|^2, which
   // in exact arithmetic is  tol |B_i|^2 / |C_i|^2 < |eps3|^2 / |eps2|^2.
   od.sa_min.assign(xlen, INFINITY);
@@ -524,7 +711,6 @@ int MPView::precompute(int threads, OrbitData& od, int reference_mode, bool keep
     if (rfe_less_host(t, runf)) runf = t;
     od.sa_min_fe[i] = runf;
   }
-  return 0;
 }
 
 int MPView::precompute_center_orbit(OrbitData& od, unsigned long orbit_bits) {

@@ -130,8 +130,14 @@ class MPView {
 
   // findProbe + computeSeries (mandelbrot.cpp:73-131), probes on `threads`
   // host threads (or the view center only, REFERENCE_CENTER).  Fills `out`.
+  // The probe lengths can be handed to `probe_lengths` (records of the probe
+  // points' coordinates, mp_record_words(mp_limbs_for_bits(bits())) words
+  // each); when it returns false they are found on the host threads.
+  using ProbeLengths = bool (*)(void* ctx, int limbs, const std::vector<uint64_t>& re,
+                                const std::vector<uint64_t>& im, int N, std::vector<int>& len);
   int precompute(int threads, OrbitData& out, int reference_mode = REFERENCE_PROBES,
-                 bool keep_mp = false);
+                 bool keep_mp = false, ProbeLengths probe_lengths = nullptr,
+                 void* probe_ctx = nullptr);
   // computeRow's pt.re per column and pt.im per row (mandelbrot.cpp:271,275)
   // as arbitrary-precision records (mp_record) of mp_limbs_for_bits(bits())
   // limbs.
@@ -152,6 +158,9 @@ class MPView {
 
  private:
   void set_precision();  // mandelbrot.cpp:37-56
+  // The series thresholds of od (sa_min, sa_fp64_ok, sa_min_fe) from its
+  // coefficients.
+  void finish_thresholds(OrbitData& od) const;
   void coord_re(int c, Mpf& out, Mpf& tmp) const;
   void coord_im(int r, Mpf& out, Mpf& tmp) const;
 

@@ -24,8 +24,8 @@ namespace nmg {
 namespace {
 
 template <int P>
-__device__ __forceinline__ Mpf<P> load_mp(const uint64_t* rec) {
-  Mpf<P> x;
+__device__ __forceinline__ Mpfx<P> load_mp(const uint64_t* rec) {
+  Mpfx<P> x;
   const uint64_t h = rec[0];
   x.e = (int32_t)(h >> 32);
   x.s = (int32_t)(uint32_t)h;
@@ -42,8 +42,8 @@ __device__ __forceinline__ const uint64_t* mp_rec(const uint64_t* base, long lon
 // Y = X[k] + d (mandelbrot.cpp:184-185, 189-190, 202-203): d set exactly
 // (mpf_set_d) and added in the view's precision.
 template <int P>
-__device__ __forceinline__ void x_plus_d(const DeviceView& v, int k, C64 d, Mpf<P>& yr,
-                                         Mpf<P>& yi) {
+__device__ __forceinline__ void x_plus_d(const DeviceView& v, int k, C64 d, Mpfx<P>& yr,
+                                         Mpfx<P>& yi) {
   yr = mpf_add(load_mp<P>(mp_rec<P>(v.x_mp, 2ll * k)), mpf_from_double<P>(d.re));
   yi = mpf_add(load_mp<P>(mp_rec<P>(v.x_mp, 2ll * k + 1)), mpf_from_double<P>(d.im));
 }
@@ -51,7 +51,7 @@ __device__ __forceinline__ void x_plus_d(const DeviceView& v, int k, C64 d, Mpf<
 template <int P>
 struct MpJob {
   struct State {
-    Mpf<P> yr, yi, y0r, y0i;
+    Mpfx<P> yr, yi, y0r, y0i;
     int32_t i;
   };
   static constexpr bool kCertifies = false;
@@ -80,7 +80,7 @@ struct MpJob {
     if (mpf_bailed_out(st.yr, st.yi)) {  // :186-207
       int low = 0, high = dsize - 1, mid = dsize / 2;
       while (low <= high) {
-        Mpf<P> mr, mi;
+        Mpfx<P> mr, mi;
         x_plus_d<P>(v, mid, sa_value(v, mid, eps, eps2, eps3), mr, mi);
         if (!mpf_bailed_out(mr, mi))
           low = mid + 1;
@@ -113,7 +113,7 @@ struct MpJob {
         executed += k;
         return true;
       }
-      Mpf<P> nr, ni;
+      Mpfx<P> nr, ni;
       mpf_orbit_step(st.yr, st.yi, st.y0r, st.y0i, nr, ni);
       double r2 = 0.0;
       if (mpf_bailed_out(nr, ni, &r2)) {
@@ -163,6 +163,26 @@ struct HwMpJob {
   }
 };
 
+// findProbe's orbit lengths (mandelbrot.cpp:85-94, computeOrbit :97-110): one
+// thread per probe point, in the view's arbitrary precision.
+template <int P>
+__global__ void __launch_bounds__(128) probe_kernel(const uint64_t* re, const uint64_t* im,
+                                                      int n, int N, int32_t* len) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const Mpfx<P> cr = load_mp<P>(mp_rec<P>(re, k)), ci = load_mp<P>(mp_rec<P>(im, k));
+  Mpfx<P> xr = cr, xi = ci;
+  int i = 1;
+  for (; i < N; i++) {
+    Mpfx<P> nr, ni;
+    mpf_orbit_step(xr, xi, cr, ci, nr, ni);
+    if (mpf_bailed_out(nr, ni)) break;
+    xr = nr;
+    xi = ni;
+  }
+  len[k] = i;
+}
+
 template <int P>
 __global__ void __launch_bounds__(kPersistentThreads) mp_kernel(DeviceView v, RenderCtl ctl,
                                                                   int chunk) {
@@ -210,7 +230,26 @@ cudaError_t dispatch(KernelKind kind, const DeviceView& v, const RenderCtl& ctl,
   }
 }
 
+template <int P>
+cudaError_t probes_p(int limbs, const uint64_t* re, const uint64_t* im, int n, int N,
+                     int32_t* len, cudaStream_t s) {
+  if constexpr (P + 1 > kMpMaxLimbs) {
+    return cudaErrorInvalidValue;
+  } else {
+    if (limbs != P + 1) return probes_p<P + 1>(limbs, re, im, n, N, len, s);
+    probe_kernel<P><<<(n + 127) / 128, 128, 0, s>>>(re, im, n, N, len);
+    return cudaGetLastError();
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_probes(int limbs, const uint64_t* re, const uint64_t* im, int n, int N,
+                          int32_t* len, cudaStream_t stream) {
+  if (limbs < kMpMinLimbs || limbs > kMpMaxLimbs || n < 1) return cudaErrorInvalidValue;
+  note_launches(1);
+  return probes_p<kMpMinLimbs - 1>(limbs, re, im, n, N, len, stream);
+}
 
 cudaError_t launch_mp(KernelKind kind, const DeviceView& v, const RenderCtl& ctl,
                       cudaStream_t stream, int blocks, int chunk) {

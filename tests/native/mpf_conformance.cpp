@@ -20,7 +20,7 @@
 #include "gmp_abi.h"
 #include "mpf_fixed.cuh"
 
-using nmg::Mpf;
+using nmg::Mpfx;
 
 namespace {
 
@@ -39,9 +39,9 @@ uint64_t rand_limb() {
 }
 
 template <int P>
-Mpf<P> rand_mpf(int max_limbs, int exp_lo, int exp_hi) {
-  Mpf<P> x = nmg::mpf_zero<P>();
-  const int n = 1 + (int)(rng() % (unsigned)(max_limbs < Mpf<P>::D ? max_limbs : Mpf<P>::D));
+Mpfx<P> rand_mpf(int max_limbs, int exp_lo, int exp_hi) {
+  Mpfx<P> x = nmg::mpf_zero<P>();
+  const int n = 1 + (int)(rng() % (unsigned)(max_limbs < Mpfx<P>::D ? max_limbs : Mpfx<P>::D));
   for (int i = 0; i < n; i++) x.d[i] = rand_limb();
   if (x.d[0] == 0) x.d[0] = 1 + (rng() & 0xffff);
   x.e = exp_lo + (int)(rng() % (unsigned)(exp_hi - exp_lo + 1));
@@ -52,20 +52,20 @@ Mpf<P> rand_mpf(int max_limbs, int exp_lo, int exp_hi) {
 // A value close to x: some limbs replaced, or the (1, 0..0) / (0, ff..ff)
 // pattern that cancels with borrows.
 template <int P>
-Mpf<P> near(const Mpf<P>& x) {
-  Mpf<P> y = x;
+Mpfx<P> near(const Mpfx<P>& x) {
+  Mpfx<P> y = x;
   const int kind = (int)(rng() % 3);
   if (kind == 0) {
-    for (int i = 0; i < Mpf<P>::D; i++)
+    for (int i = 0; i < Mpfx<P>::D; i++)
       if (rng() % 3 == 0) y.d[i] = rand_limb();
   } else {
-    const int at = (int)(rng() % Mpf<P>::D);
+    const int at = (int)(rng() % Mpfx<P>::D);
     if (y.d[at] == 0) y.d[at] = 1;
     y.d[at] -= 1;
-    for (int i = at + 1; i < Mpf<P>::D; i++) y.d[i] = (rng() % 5) ? ~0ull : rand_limb();
+    for (int i = at + 1; i < Mpfx<P>::D; i++) y.d[i] = (rng() % 5) ? ~0ull : rand_limb();
     if (kind == 2 && at == 0 && y.d[0] == 0) {  // across the exponent step
-      for (int i = 0; i + 1 < Mpf<P>::D; i++) y.d[i] = y.d[i + 1];
-      y.d[Mpf<P>::D - 1] = rand_limb();
+      for (int i = 0; i + 1 < Mpfx<P>::D; i++) y.d[i] = y.d[i + 1];
+      y.d[Mpfx<P>::D - 1] = rand_limb();
       y.e -= 1;
     }
   }
@@ -80,8 +80,8 @@ struct G {  // an mpf_t with capacity for any operand here
 };
 
 template <int P>
-void to_gmp(const Mpf<P>& x, mpf_ptr g) {
-  int n = Mpf<P>::D;
+void to_gmp(const Mpfx<P>& x, mpf_ptr g) {
+  int n = Mpfx<P>::D;
   while (n > 0 && x.d[n - 1] == 0) n--;
   if (x.s == 0 || n == 0) {
     g->_mp_size = 0;
@@ -94,7 +94,7 @@ void to_gmp(const Mpf<P>& x, mpf_ptr g) {
 }
 
 template <int P>
-bool same(mpf_srcptr g, const Mpf<P>& x) {
+bool same(mpf_srcptr g, const Mpfx<P>& x) {
   int n = g->_mp_size < 0 ? -g->_mp_size : g->_mp_size;
   const int s = g->_mp_size < 0 ? -1 : (g->_mp_size > 0);
   // GMP may keep low zero limbs; compare values
@@ -102,14 +102,14 @@ bool same(mpf_srcptr g, const Mpf<P>& x) {
   for (int i = 0; i < n && i < 64; i++) gd[i] = g->_mp_d[n - 1 - i];
   while (n > 0 && gd[n - 1] == 0) n--;
   if (n == 0) return x.s == 0;
-  if (x.s != s || x.e != g->_mp_exp || n > Mpf<P>::D) return false;
-  for (int i = 0; i < Mpf<P>::D; i++)
+  if (x.s != s || x.e != g->_mp_exp || n > Mpfx<P>::D) return false;
+  for (int i = 0; i < Mpfx<P>::D; i++)
     if (x.d[i] != (i < n ? gd[i] : 0)) return false;
   return true;
 }
 
 template <int P>
-void report(const char* op, const Mpf<P>& a, const Mpf<P>& b, mpf_srcptr g, const Mpf<P>& m) {
+void report(const char* op, const Mpfx<P>& a, const Mpfx<P>& b, mpf_srcptr g, const Mpfx<P>& m) {
   if (++failures > 10) return;
   std::printf("MISMATCH P=%d %s\n", P, op);
   auto show = [](const char* t, int s, long e, const uint64_t* d, int n) {
@@ -117,13 +117,13 @@ void report(const char* op, const Mpf<P>& a, const Mpf<P>& b, mpf_srcptr g, cons
     for (int i = 0; i < n; i++) std::printf(" %016llx", (unsigned long long)d[i]);
     std::printf(" ]\n");
   };
-  show("a", a.s, a.e, a.d, Mpf<P>::D);
-  show("b", b.s, b.e, b.d, Mpf<P>::D);
+  show("a", a.s, a.e, a.d, Mpfx<P>::D);
+  show("b", b.s, b.e, b.d, Mpfx<P>::D);
   uint64_t gd[64] = {0};
   const int n = g->_mp_size < 0 ? -g->_mp_size : g->_mp_size;
   for (int i = 0; i < n && i < 64; i++) gd[i] = g->_mp_d[n - 1 - i];
   show("gmp", g->_mp_size < 0 ? -1 : (g->_mp_size > 0), g->_mp_exp, gd, n);
-  show("here", m.s, m.e, m.d, Mpf<P>::D);
+  show("here", m.s, m.e, m.d, Mpfx<P>::D);
 }
 
 template <int P>
@@ -137,15 +137,15 @@ void check_ops(long cases) {
   }
   mpf_set_d(two.v, 2.0);
   for (long it = 0; it < cases; it++) {
-    Mpf<P> a = rand_mpf<P>(Mpf<P>::D, -3, 3);
-    Mpf<P> b = (rng() % 2) ? near(a) : rand_mpf<P>(Mpf<P>::D, a.e - 3, a.e + 1);
+    Mpfx<P> a = rand_mpf<P>(Mpfx<P>::D, -3, 3);
+    Mpfx<P> b = (rng() % 2) ? near(a) : rand_mpf<P>(Mpfx<P>::D, a.e - 3, a.e + 1);
     if (rng() % 4 == 0) b.s = -a.s;
     if (rng() % 16 == 0) b = nmg::mpf_zero<P>();
     to_gmp(a, u.v);
     to_gmp(b, v.v);
     // mul
     mpf_mul(r.v, u.v, v.v);
-    Mpf<P> m = nmg::mpf_mul(a, b);
+    Mpfx<P> m = nmg::mpf_mul(a, b);
     checked++;
     if (!same(r.v, m)) report("mul", a, b, r.v, m);
     // add
@@ -169,8 +169,20 @@ void check_ops(long cases) {
     if ((gc > 0) - (gc < 0) != hc) {
       if (++failures <= 10) std::printf("MISMATCH P=%d cmp\n", P);
     }
-    // get_d (values in the normal range)
-    if (a.e > -15 && a.e < 15) {
+    // get_d_2exp (any exponent)
+    {
+      long ge = 0, he = 0;
+      const double gm = mpf_get_d_2exp(&ge, u.v), hm = nmg::mpf_get_d_2exp(&he, a);
+      checked++;
+      if ((std::memcmp(&gm, &hm, 8) != 0 || ge != he) && ++failures <= 10)
+        std::printf("MISMATCH P=%d get_d_2exp %a %ld / %a %ld\n", P, gm, ge, hm, he);
+    }
+    // get_d, also below and above the double range
+    {
+      if (rng() % 4 == 0) {
+        a.e = (rng() & 1) ? -14 - (int)(rng() % 6) : 14 + (int)(rng() % 4);
+        to_gmp(a, u.v);
+      }
       const double gd = mpf_get_d(u.v), hd = nmg::mpf_get_d(a);
       checked++;
       if (std::memcmp(&gd, &hd, 8) != 0 && ++failures <= 10)
@@ -185,7 +197,7 @@ void check_ops(long cases) {
     if (!std::isfinite(x)) continue;
     if (rng() % 2) x = std::ldexp((double)(rng() >> 11), (int)(rng() % 200) - 150);
     mpf_set_d(r.v, x);
-    const Mpf<P> m = nmg::mpf_from_double<P>(x);
+    const Mpfx<P> m = nmg::mpf_from_double<P>(x);
     checked++;
     if (!same(r.v, m)) {
       if (++failures <= 10) std::printf("MISMATCH P=%d set_d %a\n", P, x);
@@ -206,8 +218,8 @@ void check_orbits(int orbits, int steps) {
     // random low limbs below the double
     const double base_r = -0.7436438870371510 + std::ldexp((double)(int64_t)(rng() >> 20), -60);
     const double base_i = 0.1318259042053300 + std::ldexp((double)(int64_t)(rng() >> 20), -60);
-    Mpf<P> hr = nmg::mpf_from_double<P>(base_r), hi = nmg::mpf_from_double<P>(base_i);
-    for (int i = 2; i < Mpf<P>::D; i++) {
+    Mpfx<P> hr = nmg::mpf_from_double<P>(base_r), hi = nmg::mpf_from_double<P>(base_i);
+    for (int i = 2; i < Mpfx<P>::D; i++) {
       hr.d[i] = rng();
       hi.d[i] = rng();
     }
@@ -215,7 +227,7 @@ void check_orbits(int orbits, int steps) {
     to_gmp(hi, ci.v);
     mpf_set(xr.v, cr.v);
     mpf_set(xi.v, ci.v);
-    Mpf<P> zr = hr, zi = hi;
+    Mpfx<P> zr = hr, zi = hi;
     for (int i = 0; i < steps; i++) {
       mpf_mul(t1.v, xr.v, xr.v);
       mpf_mul(t2.v, xi.v, xi.v);
@@ -224,7 +236,7 @@ void check_orbits(int orbits, int steps) {
       mpf_mul(t3.v, two.v, t3.v);
       mpf_add(nr.v, t1.v, cr.v);
       mpf_add(ni.v, t3.v, ci.v);
-      Mpf<P> mr, mi;
+      Mpfx<P> mr, mi;
       nmg::mpf_orbit_step(zr, zi, hr, hi, mr, mi);
       checked++;
       if (!same(nr.v, mr) || !same(ni.v, mi)) {

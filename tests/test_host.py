@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 import newman_gb300 as nm
-from helpers import C2, setup_oracle, shrink
+from helpers import step_for, C2, setup_oracle, shrink
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
@@ -76,6 +76,51 @@ def test_precompute_matches_oracle(oracle_mod, shape, N):
     assert m.stat(nm.STAT_ORBIT_LENGTH) == o.orbit_length
     assert m.stat(nm.STAT_PROBE_INDEX) == o.probe_index
     assert m.stat(nm.STAT_PRECISION_BITS) == o.bits
+
+
+# Deep views at increasing precision: 64, 86 and 130 bits, 300 bits by the
+# precision floor, and the 1100-bit view at width 1e-300 (seeded boundary
+# walk) with its orbit at the view center.
+DEEP_CASES = [("1e-15", 96, 0, 30000, False), ("1e-25", 96, 0, 30000, False),
+              ("1e-38", 128, 0, 30000, False), ("1e-15", 96, 300, 20000, False),
+              ("c3", 64, 1100, 200000, True)]
+
+
+@pytest.mark.parametrize("width,cols,min_bits,N,center", DEEP_CASES)
+def test_precompute_tables_match_oracle(oracle_mod, width, cols, min_bits, N, center):
+    """The probe search, the winner's orbit and its series computed by the
+    library (fixed-precision limbs, GMP's results reproduced) against the
+    oracle's GMP calls: every exported double identical."""
+    import json, os
+    from decimal import Decimal, getcontext
+    cre, cim = C2["cre"], C2["cim"]
+    if width == "c3":
+        walk = json.load(open(os.path.join(os.path.dirname(__file__), "golden",
+                                           "deep_centers.json")))["steps"]
+        getcontext().prec = 400
+        cre, cim = walk[71]["next_center_re"], walk[71]["next_center_im"]
+        step = str(Decimal(walk[72]["width"]) / cols)
+    else:
+        step = step_for(width, cols)
+    m = nm.Mandelbrot(48, cols)
+    m.set_view(cre, cim, step, step, N, 1e-10, min_bits)
+    m.set_path(nm.PATH_FP64)
+    if center:
+        m.set_option(nm.OPT_REFERENCE, nm.REFERENCE_CENTER)
+    m.precompute()
+    o = oracle_mod.OracleView(48, cols)
+    o.set_view(cre, cim, step, step, N, 1e-10, min_bits)
+    o.precompute(center=center)
+    assert m.stat(nm.STAT_PRECISION_BITS) == o.bits
+    assert m.stat(nm.STAT_ORBIT_LENGTH) == o.orbit_length > 100
+    if not center:
+        assert m.stat(nm.STAT_PROBE_INDEX) == o.probe_index
+    got = m.orbit()
+    ref = o.export_orbit()
+    for name, g in zip(("x", "xlo", "a", "b", "c"), got):
+        r = ref[name]
+        same = (g.view(np.uint64) == r.view(np.uint64)) | (np.isnan(g) & np.isnan(r))
+        assert same.all(), "%s differs at %d entries" % (name, (~same).sum())
 
 
 def test_point_at_and_view_edits(oracle_mod):

@@ -276,7 +276,7 @@ def mp_path(nm, stream, flush):
             "precision_bits": m.stat(nm.STAT_PRECISION_BITS)}, g
 
 
-def c3_deep(nm, steps, flush, stream):
+def c3_deep(nm, steps, flush, stream, args=None):
     """The 3840x2160 view at width 1e-300 (N 1,000,000, 1100-bit orbit at the
     view center, floatexp series; seeded boundary-following center): the FE32
     frame timed over `steps` renders, and the plain FP64 path over the WHOLE
@@ -291,6 +291,7 @@ def c3_deep(nm, steps, flush, stream):
     m.set_path(nm.PATH_FE32)
     m.set_option(nm.OPT_REFERENCE, nm.REFERENCE_CENTER)
     m.set_option(nm.OPT_KEEP_SMOOTH64, 1)
+    apply_orbit_options(nm, m, args)
     t0 = time.perf_counter()
     m.precompute()
     precompute_s = time.perf_counter() - t0
@@ -343,6 +344,15 @@ def c3_deep(nm, steps, flush, stream):
             "executed_iters_per_s": executed / (fe_ms * 1e-3),
             "fp64_rework_samples": rework, "wait_timeouts": timeouts,
             "interior_fraction": float((g["iterations"] == N).mean())}
+
+
+def apply_orbit_options(nm, m, args):
+    """--orbit-stage / --l2-window: the FE32 iteration pass's staged orbit
+    prefix and persisting L2 window (library defaults when not given)."""
+    if getattr(args, "orbit_stage", None) is not None:
+        m.set_option(nm.OPT_ORBIT_STAGE, args.orbit_stage)
+    if getattr(args, "l2_window", None) is not None:
+        m.set_option(nm.OPT_L2_WINDOW, args.l2_window)
 
 
 def torch_stream(stream):
@@ -399,6 +409,7 @@ def run_ours(args):
         m.set_view(CENTER[0], CENTER[1], step, step, N_ITER, TOL)
         m.scaleUp(SC)
         m.set_path(path)
+        apply_orbit_options(nm, m, args)
         return m
 
     primary = nm.PATH_FE32 if args.path == "fe32" else nm.PATH_FP64
@@ -572,7 +583,7 @@ def run_ours(args):
                                               "getIterations (MP continuation), 1 thread" % px}
             line["c1_double_loop"] = c1_double_loop(nm)
         if not args.no_deep:
-            line["c3_deep"] = c3_deep(nm, max(1, min(args.steps, 5)), flush, stream)
+            line["c3_deep"] = c3_deep(nm, max(1, min(args.steps, 5)), flush, stream, args)
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -714,6 +725,7 @@ def run_deep(args):
         m.set_view(cre, cim, step, step, N, TOL, bits)
         m.set_path(path)
         m.set_option(nm.OPT_REFERENCE, nm.REFERENCE_CENTER)
+        apply_orbit_options(nm, m, args)
         return m
 
     m = make(nm.PATH_FE32)
@@ -959,6 +971,10 @@ def main():
     ap.add_argument("--deep-band", type=int, default=16,
                     help="deep workload: the FP64 comparison renders 1/DEEP_BAND of the rows")
     ap.add_argument("--frames", type=int, default=240)
+    ap.add_argument("--orbit-stage", type=int, default=None,
+                    help="FE32: orbit entries staged in shared memory (NM_OPT_ORBIT_STAGE)")
+    ap.add_argument("--l2-window", type=int, default=None,
+                    help="FE32: 1 = persisting L2 window on the orbit (NM_OPT_L2_WINDOW)")
     ap.add_argument("--autotune", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":

@@ -79,8 +79,14 @@ enum nm_option {
   NM_OPT_FE32_OVERLAP = 10, /* FE32 passes: 1 render the uncertified samples in FP64 inside
                               the iteration pass, as they appear (default); 0 after it */
   NM_OPT_LOG_TILE_COSTS = 11, /* 1: whole-grid renders log every tile's work (nm_get_tile_costs) */
-  NM_OPT_BATCH_FP64_WARPS = 12 /* batches: warps of 8 a block on the FP64 side of the FE32 pass
+  NM_OPT_BATCH_FP64_WARPS = 12, /* batches: warps of 8 a block on the FP64 side of the FE32 pass
                                   (2, 4 or 6; 0 = 4 with double-loop frames, else 2) */
+  NM_OPT_ORBIT_STAGE = 13,  /* FE32 iteration pass: the first n (0..3072) reference-orbit entries
+                               copied into each block's shared memory by the TMA unit, where
+                               every rebased sample restarts (0: none) */
+  NM_OPT_L2_WINDOW = 14     /* FE32 iteration pass: 1 runs it with a persisting L2 access-policy
+                               window over the reference orbit (the process's L2 set-aside is
+                               raised to the orbit's size, within the device's limit) */
 };
 
 enum nm_stat {
@@ -91,6 +97,7 @@ enum nm_stat {
   NM_STAT_FP64_REWORK = 4,        /* FE32 samples not certified, re-rendered in FP64 */
   NM_STAT_WAIT_TIMEOUTS = 5,      /* overlapped FP64 rework: bounded waits that ran out (0) */
   NM_STAT_FRONT_FP64 = 6,         /* FE32 samples whose series front fell back to FP64 */
+  NM_STAT_STAGE_FALLBACKS = 7,    /* blocks that copied the staged orbit themselves (0) */
   NM_STAT_ORBIT_LENGTH = 16,      /* X.size() of the last precompute */
   NM_STAT_PROBE_INDEX = 17,       /* winning probe of findProbe */
   NM_STAT_PRECISION_BITS = 18,    /* arbitrary precision of the view */

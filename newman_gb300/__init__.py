@@ -21,10 +21,10 @@ NM_OK, NM_ERR_ARG, NM_ERR_PARSE, NM_ERR_STATE, NM_ERR_CUDA, NM_ERR_CANCELLED, NM
 PATH_REFERENCE, PATH_FP64, PATH_FE32, PATH_MP = 0, 1, 2, 3
 OPT_TILE_W, OPT_TILE_H, OPT_CHUNK, OPT_KEEP_SMOOTH64, OPT_THREADS, OPT_BLOCKS, OPT_RENORM, \
     OPT_FE32_SINGLE_PASS, OPT_REFERENCE, OPT_BATCH_GRAPH, OPT_FE32_OVERLAP, \
-    OPT_LOG_TILE_COSTS, OPT_BATCH_FP64_WARPS = range(13)
+    OPT_LOG_TILE_COSTS, OPT_BATCH_FP64_WARPS, OPT_ORBIT_STAGE, OPT_L2_WINDOW = range(15)
 REFERENCE_PROBES, REFERENCE_CENTER = 0, 1
 STAT_CARDIOID_UNDECIDED, STAT_EXECUTED_ITERS, STAT_SAMPLES, STAT_REBASES, STAT_FP64_REWORK, \
-    STAT_WAIT_TIMEOUTS, STAT_FRONT_FP64 = range(7)
+    STAT_WAIT_TIMEOUTS, STAT_FRONT_FP64, STAT_STAGE_FALLBACKS = range(8)
 STAT_ORBIT_LENGTH, STAT_PROBE_INDEX, STAT_PRECISION_BITS, STAT_PRECOMPUTE_US = 16, 17, 18, 19
 STAT_KERNEL_NS, STAT_REWORK_KERNEL_NS, STAT_ITER_KERNEL_NS, STAT_KERNEL_LAUNCHES = 20, 21, 22, 23
 

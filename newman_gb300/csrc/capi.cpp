@@ -154,12 +154,14 @@ int do_upload(nm_handle* h) {
     };
     if ((rc = upload(h->d_eps_re, h->eps_re, h->stream))) return rc;
     if ((rc = upload(h->d_eps_im, h->eps_im, h->stream))) return rc;
-    if ((rc = upload(h->d_z, cv(h->od.z), h->stream))) return rc;
-    std::vector<nmg::Flt4> zf(h->od.z.size());
-    for (size_t k = 0; k < zf.size(); k++) {
+    const size_t zlen = h->od.z.size();
+    std::vector<nmg::Flt4> zf(2 * zlen);
+    for (size_t k = 0; k < zlen; k++) {
       const float hx = (float)h->od.z[k].x, hy = (float)h->od.z[k].y;
       zf[k] = {hx, hy, (float)(h->od.z[k].x - hx), (float)(h->od.z[k].y - hy)};
     }
+    static_assert(sizeof(nmg::Flt4) == sizeof(Dbl2), "orbit entries");
+    std::memcpy(zf.data() + zlen, h->od.z.data(), zlen * sizeof(Dbl2));
     if ((rc = upload(h->d_zf, zf, h->stream))) return rc;
     if ((rc = upload(h->d_xhi, cv(h->od.xhi), h->stream))) return rc;
     if ((rc = upload(h->d_xlo, cv(h->od.xlo), h->stream))) return rc;
@@ -330,7 +332,7 @@ int nmg::prepare_view(nm_handle* h, int r0, int r1, nmg::DeviceView& v, nmg::Ker
   if (!hw) {
     v.eps_re = h->d_eps_re.p;
     v.eps_im = h->d_eps_im.p;
-    v.z = h->d_z.p;
+    v.z = h->orbit_z();
     v.zf = h->d_zf.p;
     v.zlen = (int)h->od.z.size();
     v.xlen = h->od.xlen;
@@ -418,6 +420,8 @@ nm_handle* nm_copy(const nm_handle* src) {
   h->reference_mode = src->reference_mode;
   h->fe_single_pass = src->fe_single_pass;
   h->fe_overlap = src->fe_overlap;
+  h->z_stage = src->z_stage;
+  h->l2_window = src->l2_window;
   h->tile_order = src->tile_order;
   h->tile_order_w = src->tile_order_w;
   h->tile_order_h = src->tile_order_h;
@@ -543,6 +547,13 @@ int nm_set_option(nm_handle* h, int opt, long long value) {
       return NM_OK;
     case NM_OPT_LOG_TILE_COSTS:
       h->log_costs = value != 0;
+      return NM_OK;
+    case NM_OPT_ORBIT_STAGE:
+      if (value < 0 || value > 3072) return fail(NM_ERR_ARG, "orbit stage %lld (0..3072)", value);
+      h->z_stage = (int)value;
+      return NM_OK;
+    case NM_OPT_L2_WINDOW:
+      h->l2_window = value != 0;
       return NM_OK;
     case NM_OPT_REFERENCE:
       if (value != nmg::REFERENCE_PROBES && value != nmg::REFERENCE_CENTER)
@@ -756,7 +767,8 @@ int nm_render_rows(nm_handle* h, int r0, int r1, void* stream_arg) {
       o.chunk = h->chunk;
     }
     NM_CUDA(nmg::launch_fe32_passes(v, b, ctl, s, h->device, h->blocks, chunk, h->ev[3],
-                                    h->ev[4], h->fe_overlap ? &o : nullptr));
+                                    h->ev[4], h->fe_overlap ? &o : nullptr, h->z_stage,
+                                    h->l2_window));
     h->timed_iter = true;
     h->last_overlapped = h->fe_overlap;
     h->last_view = v;
@@ -1123,7 +1135,7 @@ int noalloc_view(nm_handle* h, DeviceView& v, int& device, std::string& why, Ker
   v.coord_im = h->d_coord_im.p;
   v.eps_re = h->d_eps_re.p;
   v.eps_im = h->d_eps_im.p;
-  v.z = h->d_z.p;
+  v.z = h->orbit_z();
   v.zf = h->d_zf.p;
   v.zlen = (int)h->od.z.size();
   v.xlen = h->od.xlen;

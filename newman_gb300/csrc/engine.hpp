@@ -15,6 +15,7 @@ enum StatIndex {
   STAT_REWORK = 4,              // samples the FE32 kernel handed to the FP64 kernel
   STAT_WAIT_TIMEOUTS = 5,       // bounded waits of the overlapped rework that ran out
   STAT_FRONT_FP64 = 6,          // FE32 samples whose series front needed FP64
+  STAT_STAGE_FALLBACKS = 7,     // blocks whose staged orbit copy they made themselves
   STAT_COUNT = 8
 };
 
@@ -87,10 +88,14 @@ constexpr unsigned int kListSentinel = 0xffffffffu;
 // front pass -> iteration pass (persistent, events around it if given).  ctl
 // carries the counters, the stats and the rework list; with `overlap` the
 // iteration pass also renders the rework list in FP64 as it grows.
+// z_stage > 0: the iteration pass stages orbit entries [0, z_stage) in
+// shared memory (orbit_stage.cuh); l2_window: it runs with a persisting L2
+// access-policy window over the orbit (both copies, 32 zlen bytes).
 cudaError_t launch_fe32_passes(const DeviceView& v, const FePassBuffers& b, const RenderCtl& ctl,
                                cudaStream_t stream, int device, int blocks, int chunk,
                                cudaEvent_t iter_begin, cudaEvent_t iter_end,
-                               const OverlapCtl* overlap);
+                               const OverlapCtl* overlap, int z_stage = 0,
+                               bool l2_window = false);
 
 // ---- batches of frames (render_batch.cu) ------------------------------------
 // Frames rendered by one kernel: global sample index g of frame f runs over

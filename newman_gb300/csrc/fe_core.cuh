@@ -107,7 +107,7 @@ struct ZFF {  // reference orbit element, float-float
 };
 
 __device__ __forceinline__ ZFF fe_load_z(const DeviceView& v, int j) {
-  const Flt4 z = v.zf[j];
+  const Flt4 z = orbit_zf(v, j);
   return ZFF{z.x, z.y, z.z, z.w};
 }
 

@@ -94,8 +94,14 @@ struct nm_handle {
   bool uploaded = false;      // device copies current
   bool outside_cardioid = false;
   double precompute_us = 0.0;
-  DevBuf<Dbl2> d_coord_re, d_coord_im, d_z, d_xhi, d_xlo, d_a, d_b, d_c;
+  DevBuf<Dbl2> d_coord_re, d_coord_im, d_xhi, d_xlo, d_a, d_b, d_c;
+  // the reference orbit, zlen entries as float-float (zf) followed by zlen as
+  // FP64 pairs (z): one allocation, so that one L2 access-policy window covers
+  // both copies
   DevBuf<nmg::Flt4> d_zf;
+  const Dbl2* orbit_z() const {
+    return reinterpret_cast<const Dbl2*>(d_zf.p ? d_zf.p + od.z.size() : nullptr);
+  }
   DevBuf<double> d_eps_re, d_eps_im, d_sa_min;
   // floatexp tables (views outside the FP64 range)
   std::vector<nmg::RFE> eps_re_fe, eps_im_fe;
@@ -109,6 +115,10 @@ struct nm_handle {
   DevBuf<nmg::CFFE> d_a32, d_b32, d_c32;
   DevBuf<nmg::TFE> d_sa_min32;
   int reference_mode = nmg::REFERENCE_PROBES;
+  // FE32 iteration pass: orbit entries staged in shared memory by the TMA unit
+  // (orbit_stage.cuh), and a persisting L2 access-policy window on the orbit
+  int z_stage = 0;
+  bool l2_window = false;
 
   // scratch: work counters, statistics, and the FE32 rework list
   DevBuf<unsigned long long> d_scratch;  // kScratchWords, layout below

@@ -444,10 +444,10 @@ NM_HD bool delta_steps(const DeviceView& v, DeltaState& st, int steps, EscapeVal
   int j = st.j, i = st.i;
   const int zlast = v.zlen - 1;
   const int stop = (v.N - i < steps) ? v.N : i + steps;
-  Dbl2 z = v.z[j];
+  Dbl2 z = orbit_z(v, j);
   for (; i < stop; i++) {
     // the next orbit element, loaded before the step's arithmetic
-    const Dbl2 zn = v.z[j < zlast ? j + 1 : zlast];
+    const Dbl2 zn = orbit_z(v, j < zlast ? j + 1 : zlast);
     double tr = add_(twice_(z.x), dr);
     double ti = add_(twice_(z.y), di);
     double nre = add_(sub_(mul_(tr, dr), mul_(ti, di)), st.er);
@@ -471,7 +471,7 @@ NM_HD bool delta_steps(const DeviceView& v, DeltaState& st, int steps, EscapeVal
       dr = yr;
       di = yi;
       j = 0;
-      z = v.z[0];
+      z = orbit_z(v, 0);
     }
   }
   st.dr = dr;

@@ -29,6 +29,7 @@
 #include "engine.hpp"
 #include "fe_core.cuh"
 #include "jobs_fp64.cuh"
+#include "orbit_stage.cuh"
 #include "persistent.cuh"
 
 namespace nmg {
@@ -217,6 +218,7 @@ __device__ __noinline__ void overlap_fp64_side(const DeviceView& v, const Overla
 __global__ void __launch_bounds__(kPersistentThreads, 4) fe_overlap_kernel(
     DeviceView v, FePassBuffers b, RenderCtl ctl, OverlapCtl o, int chunk) {
   __shared__ SamplePool<Fp64AnyJob::State> pool;
+  stage_orbit_prefix(v, ctl.stats + STAT_STAGE_FALLBACKS);
   pool_init(&pool);
   const int warp = threadIdx.x >> 5;
   const int fe_warps = kPersistentThreads / 32 - kOverlapWarps;
@@ -228,11 +230,25 @@ __global__ void __launch_bounds__(kPersistentThreads, 4) fe_overlap_kernel(
   overlap_fp64_side(v, o, (unsigned long long)gridDim.x * fe_warps, &pool);
 }
 
-int blocks_for(const void* kernel, int threads, int device) {
+int blocks_for(const void* kernel, int threads, int device, size_t dyn_smem = 0) {
   int sms = 0, per_sm = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, dyn_smem);
   return sms * (per_sm < 1 ? 1 : per_sm);
+}
+
+// The persisting L2 set-aside of this process's context on `device`, once:
+// as much of the orbit as the device allows.  A context setting; it ends
+// with the process.
+void ensure_l2_set_aside(int device, size_t bytes) {
+  static size_t done[64] = {};
+  if (device < 0 || device >= 64 || done[device] >= bytes) return;
+  int max_persist = 0;
+  cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, device);
+  const size_t want = bytes < (size_t)max_persist ? bytes : (size_t)max_persist;
+  if (want > 0 && cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, want) == cudaSuccess)
+    done[device] = bytes;
+  cudaGetLastError();
 }
 
 }  // namespace
@@ -253,7 +269,7 @@ cudaError_t launch_fe32(const DeviceView& v, const RenderCtl& ctl, cudaStream_t 
 cudaError_t launch_fe32_passes(const DeviceView& v, const FePassBuffers& b, const RenderCtl& ctl,
                                cudaStream_t stream, int device, int blocks, int chunk,
                                cudaEvent_t iter_begin, cudaEvent_t iter_end,
-                               const OverlapCtl* overlap) {
+                               const OverlapCtl* overlap, int z_stage, bool l2_window) {
   const long long total = v.total;
   if (total <= 0) return cudaSuccess;
   note_launches(2);
@@ -264,9 +280,38 @@ cudaError_t launch_fe32_passes(const DeviceView& v, const FePassBuffers& b, cons
   it.list = b.work;
   it.count_ptr = b.work_n;
   if (overlap) {
-    const int oblocks =
-        blocks > 0 ? blocks : blocks_for((const void*)fe_overlap_kernel, kPersistentThreads, device);
-    fe_overlap_kernel<<<oblocks, kPersistentThreads, 0, stream>>>(v, b, it, *overlap, chunk);
+    DeviceView vs = v;
+    vs.z_stage = z_stage < 0 ? 0 : (z_stage > v.zlen ? v.zlen : z_stage);
+    const size_t dyn = 32 * (size_t)vs.z_stage;
+    if (dyn > 48 * 1024)
+      cudaFuncSetAttribute((const void*)fe_overlap_kernel,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    const int oblocks = blocks > 0 ? blocks
+                                   : blocks_for((const void*)fe_overlap_kernel,
+                                                kPersistentThreads, device, dyn);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(oblocks);
+    cfg.blockDim = dim3(kPersistentThreads);
+    cfg.dynamicSmemBytes = dyn;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    if (l2_window && v.zlen > 0) {
+      int max_window = 0;
+      cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, device);
+      size_t bytes = 32 * (size_t)v.zlen;  // zf, then z, in one allocation
+      if (max_window > 0 && bytes > (size_t)max_window) bytes = (size_t)max_window;
+      ensure_l2_set_aside(device, bytes);
+      attr[0].id = cudaLaunchAttributeAccessPolicyWindow;
+      attr[0].val.accessPolicyWindow.base_ptr = (void*)v.zf;
+      attr[0].val.accessPolicyWindow.num_bytes = bytes;
+      attr[0].val.accessPolicyWindow.hitRatio = 1.0f;
+      attr[0].val.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+      attr[0].val.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+    }
+    cudaError_t e = cudaLaunchKernelEx(&cfg, fe_overlap_kernel, vs, b, it, *overlap, chunk);
+    if (e != cudaSuccess) return e;
   } else {
     const int iblocks =
         blocks > 0 ? blocks : blocks_for((const void*)fe_iter_kernel, kPersistentThreads, device);

@@ -89,6 +89,8 @@ struct DeviceView {
   const Dbl2* z;           // [zlen] 0, get_d(X[k]), escaped element
   const Flt4* zf;          // [zlen] the same as float-float {hi.re, hi.im, lo.re, lo.im}
   int32_t zlen;
+  int32_t z_stage;         // entries [0, z_stage) of zf and z are also in the launch's
+                           // dynamic shared memory (orbit_stage.cuh); 0: none
   int32_t xlen;            // X.size()
   const Dbl2* xhi;         // [xlen] get_d(X[k])
   const Dbl2* xlo;         // [xlen] get_d(X[k] - xhi)
@@ -136,6 +138,27 @@ struct DeviceView {
 // issues FP64 at about 1/64 of the FP32 rate, and an FP64 step has 7-14 FP64
 // operations against about 140 FP32 instructions for an FE32 step.
 constexpr int kCostFp64Step = 8;
+
+// ---- the reference orbit, from shared memory where it is staged -------------
+// A launch with z_stage > 0 holds zf[0, z_stage) and then z[0, z_stage) at the
+// start of its dynamic shared memory (orbit_stage.cuh).
+#if defined(__CUDACC__)
+extern __shared__ __align__(16) unsigned char nm_orbit_smem[];
+#endif
+
+NM_HD Dbl2 orbit_z(const DeviceView& v, int j) {
+#if defined(__CUDA_ARCH__)
+  if (j < v.z_stage) return reinterpret_cast<const Dbl2*>(nm_orbit_smem + 16 * v.z_stage)[j];
+#endif
+  return v.z[j];
+}
+
+NM_HD Flt4 orbit_zf(const DeviceView& v, int j) {
+#if defined(__CUDA_ARCH__)
+  if (j < v.z_stage) return reinterpret_cast<const Flt4*>(nm_orbit_smem)[j];
+#endif
+  return v.zf[j];
+}
 
 // Sample index in tile order -> (r, c); false for padding past the grid edge.
 // With a tile order, the k-th tile handed out is tile_order[k].

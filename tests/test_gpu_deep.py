@@ -30,6 +30,19 @@ def view_at(k, grid):
     return cre, cim, step
 
 
+RESULTS = {}
+
+
+def _record(key, value):
+    """Keeps a measured fraction; written as JSON to the file named by the
+    environment variable NM_TEST_RECORD (with a "deep" suffix) when set."""
+    RESULTS[key] = value
+    path = os.environ.get("NM_TEST_RECORD")
+    if path:
+        with open(path + ".deep.json", "w") as f:
+            json.dump(RESULTS, f, indent=1)
+
+
 @pytest.fixture(scope="module")
 def nm():
     import newman_gb300
@@ -66,8 +79,11 @@ def test_deep_fp64_matches_oracle(nm, oracle_mod, k):
     g = m.grid()["iterations"][rows.ravel(), cols.ravel()]
     assert np.array_equal(g, it)
     assert np.abs(m.smoothing64()[rows.ravel(), cols.ravel()] - sm).max() <= 1e-12
-    mp_it, _ = o.render_pixels(rows.ravel()[:24], cols.ravel()[:24], oracle_mod.MODE_REF_FE)
-    assert (mp_it == it[:24]).mean() >= 0.75
+    # the arbitrary-precision continuation on all 576 compared samples
+    mp_it, _ = o.render_pixels(rows.ravel(), cols.ravel(), oracle_mod.MODE_REF_FE)
+    frac = float((mp_it == it).mean())
+    _record("deep_k%d_fp64_vs_mp_576" % k, frac)
+    assert frac >= 0.9
 
 
 @pytest.mark.parametrize("k", [9, 30, 72, 80, 87])

@@ -91,14 +91,18 @@ MPF_HD uint64_t subb(uint64_t a, uint64_t b, uint64_t& br) {
   return u;
 }
 
-// d[k] for a runtime k, 0 outside [0, D): selects over the limbs, so that the
-// limbs stay in registers on the GPU.
+// d[k] for a runtime k, 0 outside [0, D): on the GPU by selects over the
+// limbs, so that they stay in registers; on the host by indexing.
 template <int D>
 MPF_HD uint64_t limb_at(const uint64_t (&d)[D], int k) {
+#if defined(__CUDA_ARCH__)
   uint64_t r = 0;
 #pragma unroll
   for (int j = 0; j < D; j++) r = (k == j) ? d[j] : r;
   return r;
+#else
+  return (k >= 0 && k < D) ? d[k] : 0;
+#endif
 }
 
 }  // namespace mpf_detail

@@ -67,8 +67,11 @@ int orbit_length(mpf_srcptr cr, mpf_srcptr ci, int N, unsigned long bits) {
 // ---- the same arithmetic on fixed-precision limbs (mpf_fixed.cuh) -----------
 // GMP's results bit for bit without a library call per operation: the probe
 // search, the winner's orbit and its series run here for precisions of
-// kFixedMinP .. kFixedMaxP limbs (64 .. 1216 bits).
-constexpr int kFixedMinP = 2, kFixedMaxP = 20;
+// kFixedMinP .. kFixedMaxP limbs (64 .. 448 bits); above, GMP's own
+// multiplication is the faster (measured on the 1e-300 view's orbit and
+// series: 314 bits 0.19 s here against 0.24 s with GMP, 600 bits 0.65 s
+// against 0.50 s, 1100 bits 2.5 s against 1.6 s).
+constexpr int kFixedMinP = 2, kFixedMaxP = 8;
 
 template <int P>
 Mpfx<P> fixed_of(mpf_srcptr x) {

@@ -83,7 +83,8 @@ enum nm_option {
                                   (2, 4 or 6; 0 = 4 with double-loop frames, else 2) */
   NM_OPT_ORBIT_STAGE = 13,  /* FE32 iteration pass: the first n (0..3072) reference-orbit entries
                                copied into each block's shared memory by the TMA unit, where
-                               every rebased sample restarts (0: none) */
+                               every rebased sample restarts (0: none; -1, the default: 1024 on
+                               views whose series leaves the double range, else none) */
   NM_OPT_L2_WINDOW = 14     /* FE32 iteration pass: 1 runs it with a persisting L2 access-policy
                                window over the reference orbit (the process's L2 set-aside is
                                raised to the orbit's size, within the device's limit) */

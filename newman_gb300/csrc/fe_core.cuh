@@ -106,8 +106,9 @@ struct ZFF {  // reference orbit element, float-float
   float hx, hy, lx, ly;
 };
 
+template <bool kStaged = false>
 __device__ __forceinline__ ZFF fe_load_z(const DeviceView& v, int j) {
-  const Flt4 z = orbit_zf(v, j);
+  const Flt4 z = orbit_zf<kStaged>(v, j);
   return ZFF{z.x, z.y, z.z, z.w};
 }
 
@@ -389,13 +390,14 @@ __device__ __forceinline__ void fe_renormalise(FeState& st) {
 // Steps while delta is scaled: Y = Z to working precision, so the events are
 // the reference's own escape, the end of the orbit, and Z passing so close to
 // 0 that |Y| < |delta| could hold (left to the FP64 kernel: uncertified).
+template <bool kStaged = false>
 __device__ __forceinline__ bool fe_scaled_steps(const DeviceView& v, FeState& st, int steps,
                                              FeResult& res, unsigned long long& executed,
                                              unsigned long long& rebases) {
   const int zlast = v.zlen - 1;
   const int stop = min(v.N, st.i + steps);
   const int start = st.i;
-  ZFF z = fe_load_z(v, st.j);
+  ZFF z = fe_load_z<kStaged>(v, st.j);
   bool done = false;
   for (; st.i < stop; st.i++) {
     const FF sd_r = st.E < -140 ? FF{0.f, 0.f} : ff_scale(st.dr, st.E);
@@ -418,7 +420,7 @@ __device__ __forceinline__ bool fe_scaled_steps(const DeviceView& v, FeState& st
     st.dr = nr;
     st.di = ni;
     st.j++;
-    z = fe_load_z(v, st.j);
+    z = fe_load_z<kStaged>(v, st.j);
     const float zm2 = fmaf(z.hx, z.hx, z.hy * z.hy);
     const FF yr = ff_add(FF{z.hx, z.lx}, st.E < -140 ? FF{0.f, 0.f} : ff_scale(st.dr, st.E));
     const FF yi = ff_add(FF{z.hy, z.ly}, st.E < -140 ? FF{0.f, 0.f} : ff_scale(st.di, st.E));
@@ -479,7 +481,7 @@ __device__ __forceinline__ bool fe_scaled_steps(const DeviceView& v, FeState& st
 // the iteration stops at once and res is not meaningful -- the sample goes to
 // the FP64 kernel.
 // The unscaled steps; kDl: a double-loop view (second bound e64, trapping).
-template <bool kDl>
+template <bool kDl, bool kStaged = false>
 __device__ __forceinline__ bool fe_unscaled_steps(const DeviceView& v, FeState& st, int steps,
                                                   FeResult& res, unsigned long long& executed,
                                                   unsigned long long& rebases, FeTrap* trap) {
@@ -497,7 +499,7 @@ __device__ __forceinline__ bool fe_unscaled_steps(const DeviceView& v, FeState& 
   float rho = (kDl && trap && st.i > 0) ? trap->rho : 0.0f;
   int j = st.j, i = st.i;
   bool certified = st.certified != 0;
-  ZFF z = fe_load_z(v, j);
+  ZFF z = fe_load_z<kStaged>(v, j);
   // |Y| of the current state (for the error bound's amplification 2|Y|),
   // from the hardware reciprocal square root: within 2^-21 of |Y_h|, which
   // the 2^-20 (|Z| + |delta|) margins below cover together with the hi parts'
@@ -517,7 +519,7 @@ __device__ __forceinline__ bool fe_unscaled_steps(const DeviceView& v, FeState& 
     dr = nr;
     di = ni;
     j++;
-    z = fe_load_z(v, j);
+    z = fe_load_z<kStaged>(v, j);
     const float yr = z.hx + dr.h, yi = z.hy + di.h;
     const float r2 = fmaf(yr, yr, yi * yi);
     ym = approx_sqrt(r2);
@@ -589,7 +591,7 @@ __device__ __forceinline__ bool fe_unscaled_steps(const DeviceView& v, FeState& 
       di = nyi;
       err = yerr_fe;
       j = 0;
-      z = fe_load_z(v, 0);
+      z = fe_load_z<kStaged>(v, 0);
       ym = approx_norm(dr.h, di.h);
       rebases++;
     }
@@ -647,6 +649,7 @@ __device__ __forceinline__ bool fe_unscaled_steps(const DeviceView& v, FeState& 
   return false;
 }
 
+template <bool kStaged = false>
 __device__ __forceinline__ bool fe_advance(const DeviceView& v, FeState& st, int steps,
                                            FeResult& res, unsigned long long& executed,
                                            unsigned long long& rebases, FeTrap* trap = nullptr) {
@@ -655,10 +658,11 @@ __device__ __forceinline__ bool fe_advance(const DeviceView& v, FeState& st, int
       st.certified = 0;
       return true;
     }
-    return fe_scaled_steps(v, st, steps, res, executed, rebases);
+    return fe_scaled_steps<kStaged>(v, st, steps, res, executed, rebases);
   }
-  if (v.double_loop) return fe_unscaled_steps<true>(v, st, steps, res, executed, rebases, trap);
-  return fe_unscaled_steps<false>(v, st, steps, res, executed, rebases, nullptr);
+  if (v.double_loop)
+    return fe_unscaled_steps<true, kStaged>(v, st, steps, res, executed, rebases, trap);
+  return fe_unscaled_steps<false, kStaged>(v, st, steps, res, executed, rebases, nullptr);
 }
 
 }  // namespace nmg

@@ -117,7 +117,7 @@ struct nm_handle {
   int reference_mode = nmg::REFERENCE_PROBES;
   // FE32 iteration pass: orbit entries staged in shared memory by the TMA unit
   // (orbit_stage.cuh), and a persisting L2 access-policy window on the orbit
-  int z_stage = 0;
+  int z_stage = -1;  // -1: kAutoOrbitStage on floatexp views, else none
   bool l2_window = false;
 
   // scratch: work counters, statistics, and the FE32 rework list

@@ -38,8 +38,10 @@ struct HwJob {
 // value stays clear of the underflow range and in FP64 with an unbounded
 // exponent (pixel_xd.cuh) otherwise, moving between the two at step (plain to
 // unbounded) and chunk (back) boundaries -- the results are the unbounded
-// form's throughout.  The other views iterate in plain doubles.
-struct Delta64Job {
+// form's throughout.  The other views iterate in plain doubles.  kStaged: the
+// kernel staged the orbit's leading entries in shared memory.
+template <bool kStaged = false>
+struct Delta64JobT {
   struct State {
     union {
       DeltaState d;
@@ -70,18 +72,18 @@ struct Delta64Job {
     const int before = st.xd ? st.x.i : st.d.i;
     bool done;
     if (!v.sa_fe) {
-      done = delta_steps(v, st.d, n, out, sm);
+      done = delta_steps<kStaged>(v, st.d, n, out, sm);
     } else if (st.xd) {
-      done = delta_xd_steps(v, st.x, n, out, sm);
+      done = delta_xd_steps<kStaged>(v, st.x, n, out, sm);
       if (!done && delta_xd_to_plain(st.x, st.d)) st.xd = 0;
     } else {
       bool handover;
-      done = delta_guarded_steps(v, st.d, n, out, sm, handover);
+      done = delta_guarded_steps<kStaged>(v, st.d, n, out, sm, handover);
       if (handover) {  // the rest of the chunk in the unbounded-exponent form
         const int left = n - (st.d.i - before);
         delta_to_xd(st.d, st.x);
         st.xd = 1;
-        done = left > 0 ? delta_xd_steps(v, st.x, left, out, sm) : false;
+        done = left > 0 ? delta_xd_steps<kStaged>(v, st.x, left, out, sm) : false;
       }
     }
     const int after = st.xd ? st.x.i : st.d.i;
@@ -90,13 +92,15 @@ struct Delta64Job {
     return done;
   }
 };
+using Delta64Job = Delta64JobT<false>;
 
 // The FP64 rework of the FE32 path: the double loop on double-loop views (the
 // FE32 path's comparator there), else the FP64 perturbation path.
-struct Fp64AnyJob {
+template <bool kStaged = false>
+struct Fp64AnyJobT {
   union State {
     HwJob::State hw;
-    Delta64Job::State d;
+    typename Delta64JobT<kStaged>::State d;
   };
   static constexpr bool kCertifies = false;
   static constexpr int kCostWeight = kCostFp64Step;
@@ -104,15 +108,16 @@ struct Fp64AnyJob {
   static __device__ __forceinline__ bool init(const DeviceView& v, int r, int c, State& st,
                                               EscapeValue& out, double& sm, bool& und) {
     if (v.double_loop) return HwJob::init(v, r, c, st.hw, out, sm, und);
-    return Delta64Job::init(v, r, c, st.d, out, sm, und);
+    return Delta64JobT<kStaged>::init(v, r, c, st.d, out, sm, und);
   }
   static __device__ __forceinline__ bool steps(const DeviceView& v, State& st, int n,
                                                EscapeValue& out, double& sm,
                                                unsigned long long& executed,
                                                unsigned long long& rebases) {
     if (v.double_loop) return HwJob::steps(v, st.hw, n, out, sm, executed, rebases);
-    return Delta64Job::steps(v, st.d, n, out, sm, executed, rebases);
+    return Delta64JobT<kStaged>::steps(v, st.d, n, out, sm, executed, rebases);
   }
 };
+using Fp64AnyJob = Fp64AnyJobT<false>;
 
 }  // namespace nmg

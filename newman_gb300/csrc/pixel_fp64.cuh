@@ -438,16 +438,17 @@ NM_HD void delta_start(const SeriesFront& f, DeltaState& st) {
   st.eps_tiny = 0;
 }
 
+template <bool kStaged = false>
 NM_HD bool delta_steps(const DeviceView& v, DeltaState& st, int steps, EscapeValue& out,
                        double& sm) {
   double dr = st.dr, di = st.di;
   int j = st.j, i = st.i;
   const int zlast = v.zlen - 1;
   const int stop = (v.N - i < steps) ? v.N : i + steps;
-  Dbl2 z = orbit_z(v, j);
+  Dbl2 z = orbit_z<kStaged>(v, j);
   for (; i < stop; i++) {
     // the next orbit element, loaded before the step's arithmetic
-    const Dbl2 zn = orbit_z(v, j < zlast ? j + 1 : zlast);
+    const Dbl2 zn = orbit_z<kStaged>(v, j < zlast ? j + 1 : zlast);
     double tr = add_(twice_(z.x), dr);
     double ti = add_(twice_(z.y), di);
     double nre = add_(sub_(mul_(tr, dr), mul_(ti, di)), st.er);
@@ -471,7 +472,7 @@ NM_HD bool delta_steps(const DeviceView& v, DeltaState& st, int steps, EscapeVal
       dr = yr;
       di = yi;
       j = 0;
-      z = orbit_z(v, 0);
+      z = orbit_z<kStaged>(v, 0);
     }
   }
   st.dr = dr;

@@ -25,6 +25,7 @@ NM_HD void delta_xd_start(const SeriesFront& f, DeltaXDState& st) {
   st.i = f.dsize;
 }
 
+template <bool kStaged = false>
 NM_HD bool delta_xd_steps(const DeviceView& v, DeltaXDState& st, int steps, EscapeValue& out,
                           double& sm) {
   XD dr = st.dr, di = st.di;
@@ -32,9 +33,9 @@ NM_HD bool delta_xd_steps(const DeviceView& v, DeltaXDState& st, int steps, Esca
   const int zlast = v.zlen - 1;
   const int stop = (v.N - i < steps) ? v.N : i + steps;
   const XD bail2 = xd_of(v.bailout2);
-  Dbl2 z = orbit_z(v, j);
+  Dbl2 z = orbit_z<kStaged>(v, j);
   for (; i < stop; i++) {
-    const Dbl2 zn = orbit_z(v, j < zlast ? j + 1 : zlast);  // loaded before the step's arithmetic
+    const Dbl2 zn = orbit_z<kStaged>(v, j < zlast ? j + 1 : zlast);  // loaded before the step's arithmetic
     const XD tr = xd_add(xd_twice(xd_of(z.x)), dr);
     const XD ti = xd_add(xd_twice(xd_of(z.y)), di);
     const XD nre = xd_add(xd_sub(xd_mul(tr, dr), xd_mul(ti, di)), st.er);
@@ -60,7 +61,7 @@ NM_HD bool delta_xd_steps(const DeviceView& v, DeltaXDState& st, int steps, Esca
       dr = yr;
       di = yi;
       j = 0;
-      z = orbit_z(v, 0);
+      z = orbit_z<kStaged>(v, 0);
     }
   }
   st.dr = dr;
@@ -141,6 +142,7 @@ NM_HD bool delta_plain_start(const SeriesFront& f, DeltaState& st) {
 
 // delta_steps with the guard; `handover` is set when a step was left to the
 // unbounded-exponent form (st is the exact state before it).
+template <bool kStaged = false>
 NM_HD bool delta_guarded_steps(const DeviceView& v, DeltaState& st, int steps, EscapeValue& out,
                                double& sm, bool& handover) {
   double dr = st.dr, di = st.di;
@@ -149,9 +151,9 @@ NM_HD bool delta_guarded_steps(const DeviceView& v, DeltaState& st, int steps, E
   const int stop = (v.N - i < steps) ? v.N : i + steps;
   const bool eps_tiny = st.eps_tiny != 0;
   handover = false;
-  Dbl2 z = orbit_z(v, j);
+  Dbl2 z = orbit_z<kStaged>(v, j);
   for (; i < stop; i++) {
-    const Dbl2 zn = orbit_z(v, j < zlast ? j + 1 : zlast);  // loaded before the step's arithmetic
+    const Dbl2 zn = orbit_z<kStaged>(v, j < zlast ? j + 1 : zlast);  // loaded before the step's arithmetic
     const double tr = add_(twice_(z.x), dr);
     const double ti = add_(twice_(z.y), di);
     const double nre = add_(sub_(mul_(tr, dr), mul_(ti, di)), st.er);
@@ -182,7 +184,7 @@ NM_HD bool delta_guarded_steps(const DeviceView& v, DeltaState& st, int steps, E
       dr = yr;
       di = yi;
       j = 0;
-      z = orbit_z(v, 0);
+      z = orbit_z<kStaged>(v, 0);
     }
   }
   st.dr = dr;

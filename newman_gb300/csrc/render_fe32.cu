@@ -123,6 +123,7 @@ static_assert(sizeof(FeResult) == kFeResultBytes, "FE32 result record");
 
 // Persistent and warp-refilled like persistent_loop, over the work list: the
 // start state comes from the front pass, the result goes to the grid.
+template <bool kStaged = false>
 __device__ __forceinline__ void fe_iter_warp(const DeviceView& v, const FePassBuffers& b,
                                              const RenderCtl& ctl, int chunk) {
   const unsigned kFull = 0xffffffffu;
@@ -160,7 +161,8 @@ __device__ __forceinline__ void fe_iter_warp(const DeviceView& v, const FePassBu
     if (!__any_sync(kFull, active)) break;
     if (active) {
       FeResult res;
-      if (fe_advance(v, st, chunk, res, executed, rebases, v.trap ? v.trap + sid : nullptr)) {
+      if (fe_advance<kStaged>(v, st, chunk, res, executed, rebases,
+                              v.trap ? v.trap + sid : nullptr)) {
         int r = 0, c = 0;
         sample_rc(v, sid, r, c);
         if (st.certified) {
@@ -208,26 +210,30 @@ constexpr int kOverlapWarps = 2;
 
 // The FP64 side, out of line: its register pressure (the FP64 series front)
 // then stays out of the FP32 iteration's allocation.
+template <bool kStaged>
 __device__ __noinline__ void overlap_fp64_side(const DeviceView& v, const OverlapCtl& o,
                                                unsigned long long producers,
-                                               SamplePool<Fp64AnyJob::State>* pool) {
-  drain_loop<Fp64AnyJob>(OneView{v}, o.rework, o.fe_warps_done, producers, o.timeouts, o.chunk,
-                         pool);
+                                               SamplePool<typename Fp64AnyJobT<kStaged>::State>* pool) {
+  drain_loop<Fp64AnyJobT<kStaged>>(OneView{v}, o.rework, o.fe_warps_done, producers, o.timeouts,
+                                   o.chunk, pool);
 }
 
+// kStaged: the launch stages the orbit's first v.z_stage entries in its
+// dynamic shared memory (orbit_stage.cuh) and both sides read them there.
+template <bool kStaged>
 __global__ void __launch_bounds__(kPersistentThreads, 4) fe_overlap_kernel(
     DeviceView v, FePassBuffers b, RenderCtl ctl, OverlapCtl o, int chunk) {
-  __shared__ SamplePool<Fp64AnyJob::State> pool;
-  stage_orbit_prefix(v, ctl.stats + STAT_STAGE_FALLBACKS);
+  __shared__ SamplePool<typename Fp64AnyJobT<kStaged>::State> pool;
+  if (kStaged) stage_orbit_prefix(v, ctl.stats + STAT_STAGE_FALLBACKS);
   pool_init(&pool);
   const int warp = threadIdx.x >> 5;
   const int fe_warps = kPersistentThreads / 32 - kOverlapWarps;
   if (warp < fe_warps) {
-    fe_iter_warp(v, b, ctl, chunk);
+    fe_iter_warp<kStaged>(v, b, ctl, chunk);
     producer_warp_done(o.fe_warps_done);
     return;
   }
-  overlap_fp64_side(v, o, (unsigned long long)gridDim.x * fe_warps, &pool);
+  overlap_fp64_side<kStaged>(v, o, (unsigned long long)gridDim.x * fe_warps, &pool);
 }
 
 int blocks_for(const void* kernel, int threads, int device, size_t dyn_smem = 0) {
@@ -283,12 +289,12 @@ cudaError_t launch_fe32_passes(const DeviceView& v, const FePassBuffers& b, cons
     DeviceView vs = v;
     vs.z_stage = z_stage < 0 ? 0 : (z_stage > v.zlen ? v.zlen : z_stage);
     const size_t dyn = 32 * (size_t)vs.z_stage;
+    const void* kernel = vs.z_stage > 0 ? (const void*)fe_overlap_kernel<true>
+                                        : (const void*)fe_overlap_kernel<false>;
     if (dyn > 48 * 1024)
-      cudaFuncSetAttribute((const void*)fe_overlap_kernel,
-                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
-    const int oblocks = blocks > 0 ? blocks
-                                   : blocks_for((const void*)fe_overlap_kernel,
-                                                kPersistentThreads, device, dyn);
+      cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    const int oblocks =
+        blocks > 0 ? blocks : blocks_for(kernel, kPersistentThreads, device, dyn);
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(oblocks);
     cfg.blockDim = dim3(kPersistentThreads);
@@ -310,7 +316,10 @@ cudaError_t launch_fe32_passes(const DeviceView& v, const FePassBuffers& b, cons
       cfg.attrs = attr;
       cfg.numAttrs = 1;
     }
-    cudaError_t e = cudaLaunchKernelEx(&cfg, fe_overlap_kernel, vs, b, it, *overlap, chunk);
+    cudaError_t e = vs.z_stage > 0
+                        ? cudaLaunchKernelEx(&cfg, fe_overlap_kernel<true>, vs, b, it, *overlap, chunk)
+                        : cudaLaunchKernelEx(&cfg, fe_overlap_kernel<false>, vs, b, it, *overlap,
+                                             chunk);
     if (e != cudaSuccess) return e;
   } else {
     const int iblocks =

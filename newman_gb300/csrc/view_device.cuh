@@ -146,16 +146,21 @@ constexpr int kCostFp64Step = 8;
 extern __shared__ __align__(16) unsigned char nm_orbit_smem[];
 #endif
 
+// kStaged: the calling kernel staged the prefix (a compile-time choice, so
+// that the loads of every other kernel carry no test).
+template <bool kStaged = false>
 NM_HD Dbl2 orbit_z(const DeviceView& v, int j) {
 #if defined(__CUDA_ARCH__)
-  if (j < v.z_stage) return reinterpret_cast<const Dbl2*>(nm_orbit_smem + 16 * v.z_stage)[j];
+  if (kStaged && j < v.z_stage)
+    return reinterpret_cast<const Dbl2*>(nm_orbit_smem + 16 * v.z_stage)[j];
 #endif
   return v.z[j];
 }
 
+template <bool kStaged = false>
 NM_HD Flt4 orbit_zf(const DeviceView& v, int j) {
 #if defined(__CUDA_ARCH__)
-  if (j < v.z_stage) return reinterpret_cast<const Flt4*>(nm_orbit_smem)[j];
+  if (kStaged && j < v.z_stage) return reinterpret_cast<const Flt4*>(nm_orbit_smem)[j];
 #endif
   return v.zf[j];
 }

@@ -127,3 +127,24 @@ def test_fe32_traps_interior_orbits_of_double_loop_views(nm):
     assert interior.mean() > 0.5
     assert np.array_equal(a, b)
     assert fe.stat(nm.STAT_EXECUTED_ITERS) < 0.75 * ref.stat(nm.STAT_EXECUTED_ITERS)
+
+
+@pytest.mark.parametrize("width", ["1e-14", "1e-330"])
+def test_orbit_staging_changes_nothing(nm, width):
+    """The FE32 iteration pass with the orbit's first entries staged in shared
+    memory by the TMA unit (1024, and 3072 -- 96 KB a block), with the
+    persisting L2 window, and with neither: identical grids, and every block's
+    bulk copies arrived (no block copied the entries itself)."""
+    view = dict(C2, nr=96, nc=160, sc=2, step=step_for(width, 160), N=40000)
+    grids = []
+    for stage, l2 in ((0, 0), (1024, 0), (3072, 1)):
+        m = setup_gpu(nm, view, path=nm.PATH_FE32, keep64=False)
+        m.set_option(nm.OPT_REFERENCE, nm.REFERENCE_CENTER)
+        m.set_option(nm.OPT_ORBIT_STAGE, stage)
+        m.set_option(nm.OPT_L2_WINDOW, l2)
+        m.precompute()
+        m.render()
+        assert m.stat(nm.STAT_STAGE_FALLBACKS) == 0
+        grids.append(m.grid())
+    for g in grids[1:]:
+        assert np.array_equal(g, grids[0])

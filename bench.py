@@ -589,6 +589,61 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def run_rows(args):
+    """The C2 view split by rows across the ranks (strong scaling): every rank
+    precomputes the same view and renders its block of rows
+    (newman_gb300.shard); the step time is the slowest rank's; the rows are
+    gathered to rank 0 on the host after the timed steps and checked against
+    rank 0's own render of the whole view."""
+    import torch
+    import torch.distributed as dist
+    import newman_gb300 as nm
+    from newman_gb300.shard import gather_rows, row_range
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("gloo")
+    m = nm.Mandelbrot(NR, NC)
+    m.set_view(CENTER[0], CENTER[1], step_string(), step_string(), N_ITER, TOL)
+    m.scaleUp(SC)
+    m.set_path(nm.PATH_FE32)
+    m.precompute()
+    m.upload()
+    r0, r1 = row_range(m.rows(), rank, world)
+    stream = torch.cuda.Stream()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    times = []
+    for i in range(args.warmup + args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        e0, e1 = cuda_events()
+        if world > 1:
+            dist.barrier()
+        e0.record(stream)
+        m.render_rows(r0, r1, stream.cuda_stream)
+        e1.record(stream)
+        m.synchronize()
+        stream.synchronize()
+        if i >= args.warmup:
+            times.append(e0.elapsed_time(e1))
+    ms = max_over_ranks(float(np.mean(times))) if world > 1 else float(np.mean(times))
+    part = m.grid()[r0:r1].copy()
+    full = gather_rows(part, m.rows(), m.cols(), rank, world) if world > 1 else m.grid()
+    if rank == 0:
+        eff = int(full["iterations"].astype(np.int64).sum())
+        m.render()
+        identical = bool(np.array_equal(full, m.grid()))
+        print(json.dumps({
+            "metric": METRIC + " (one view split by rows)", "value": eff / (ms * 1e-3),
+            "unit": "pixel-iters/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "strong", "vs_baseline": None, "dtype": "fp32 float-float + int exponent",
+            "data": "synthetic view (no dataset)", "config": workload_config(),
+            "shard": "rows", "gathered_equals_whole_render": identical}), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
 def video_views(nframes, nr, nc, w0="4.0", w1="1e-200", n0=1000, n1=500000):
     """Frames of the batched zoom video: widths geometric from w0 to w1, N
     linear from n0 to n1, into the C2 center."""
@@ -971,6 +1026,8 @@ def main():
     ap.add_argument("--deep-band", type=int, default=16,
                     help="deep workload: the FP64 comparison renders 1/DEEP_BAND of the rows")
     ap.add_argument("--frames", type=int, default=240)
+    ap.add_argument("--shard", default="replicas", choices=["replicas", "rows"],
+                    help="rows: one C2 view split by rows across the ranks (strong scaling)")
     ap.add_argument("--orbit-stage", type=int, default=None,
                     help="FE32: orbit entries staged in shared memory (NM_OPT_ORBIT_STAGE)")
     ap.add_argument("--l2-window", type=int, default=None,
@@ -985,6 +1042,8 @@ def main():
         run_deep(args)
     elif args.workload == "learned":
         run_learned(args)
+    elif args.shard == "rows":
+        run_rows(args)
     else:
         run_ours(args)
 

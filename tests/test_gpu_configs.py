@@ -87,14 +87,15 @@ def test_c3_full_frame(nm, oracle_mod):
     assert bad.size == 0, "FP64 frame vs MODE_DELTA_FE: %d of 4096 differ" % bad.size
     assert np.abs(fp.smoothing64()[rr, cc] - sm).max() <= 1e-12
     # the arbitrary-precision continuation (the reference's algorithm with a
-    # floatexp series front): most samples agree; the view is chaotic at the
-    # sample scale
+    # floatexp series front): the view is chaotic at the sample scale and the
+    # perturbation's FP64 orbit (2^-53 of |X| absolute) differs from it by a
+    # few sample steps; measured 2047 of the 2048 seeded samples identical
     mp_it, _ = o.render_pixels(rr[:2048], cc[:2048], oracle_mod.MODE_REF_FE)
     frac_fp = float((g_fp[rr[:2048], cc[:2048]] == mp_it).mean())
     frac_fe = float((g_fe[rr[:2048], cc[:2048]] == mp_it).mean())
     _record("c3_fp64_vs_mp_2048", frac_fp)
     _record("c3_fe32_vs_mp_2048", frac_fe)
-    assert frac_fp >= 0.95 and frac_fe >= 0.95
+    assert frac_fp >= 0.999 and frac_fe >= 0.999
 
 
 def test_c4_240_frame_batch_equals_frames_alone(nm):

@@ -79,11 +79,13 @@ def test_deep_fp64_matches_oracle(nm, oracle_mod, k):
     g = m.grid()["iterations"][rows.ravel(), cols.ravel()]
     assert np.array_equal(g, it)
     assert np.abs(m.smoothing64()[rows.ravel(), cols.ravel()] - sm).max() <= 1e-12
-    # the arbitrary-precision continuation on all 576 compared samples
+    # the arbitrary-precision continuation on all 576 compared samples:
+    # measured 98.96 % to 100 % identical over the five views (the FP64
+    # orbit's own rounding, amplified where the views are chaotic)
     mp_it, _ = o.render_pixels(rows.ravel(), cols.ravel(), oracle_mod.MODE_REF_FE)
     frac = float((mp_it == it).mean())
     _record("deep_k%d_fp64_vs_mp_576" % k, frac)
-    assert frac >= 0.9
+    assert frac >= 0.985
 
 
 @pytest.mark.parametrize("k", [9, 30, 72, 80, 87])

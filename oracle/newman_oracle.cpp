@@ -50,7 +50,12 @@ constexpr double kMinPreview = 1.5e-16;             // mandelbrot.cpp:257
 
 // MODE_REF_FE / MODE_DELTA_FE: the same with the floatexp series front, for
 // views whose series terms leave the FP64 range.
-enum { MODE_REF = 0, MODE_DELTA = 1, MODE_REF_FE = 2, MODE_DELTA_FE = 3 };
+// MODE_DELTA_SINGLE: MODE_DELTA without the rebase on |Y| < |delta| -- plain
+// single-reference perturbation, which loses precision where a sample's orbit
+// passes far closer to 0 than the reference's (Pauldelbrot's glitches).  A
+// planted mistake for the tests to show what the rebase catches; the orbit's
+// end still rebases, so that every sample can go on.
+enum { MODE_REF = 0, MODE_DELTA = 1, MODE_REF_FE = 2, MODE_DELTA_FE = 3, MODE_DELTA_SINGLE = 4 };
 
 // RAII holder for one mpf_t at a fixed precision.
 struct MP {
@@ -475,7 +480,7 @@ Pixel get_iterations(View& v, mpf_srcptr y0r, mpf_srcptr y0i, Scratch& s) {
 // or the orbit is exhausted:
 //   t = 2 Z[j] + delta;  delta = t * delta + eps;  j += 1;  Y = Z[j] + delta
 Pixel get_iterations_delta(View& v, mpf_srcptr y0r, mpf_srcptr y0i, Scratch& s,
-                           const std::vector<LP>& Z) {
+                           const std::vector<LP>& Z, bool rebase_small = true) {
   Pixel out;
   SAState st;
   if (series_front(v, y0r, y0i, s, out, st)) return out;
@@ -495,7 +500,7 @@ Pixel get_iterations_delta(View& v, mpf_srcptr y0r, mpf_srcptr y0i, Scratch& s,
     double r2 = y.re * y.re + y.im * y.im;
     if (r2 > kBailout2) return {i, smoothing_magnitude(r2)};
     double d2 = dl.re * dl.re + dl.im * dl.im;
-    if (r2 < d2 || j == zlast) {
+    if ((rebase_small && r2 < d2) || j == zlast) {
       dl = y;
       j = 0;
     }
@@ -904,7 +909,8 @@ int nmo_render_pixels(nmo_view* h, int mode, long npix, const int32_t* rows, con
   if (!hw && !v->precomputed) return 3;
   if (mode != MODE_REF && hw) return 4;
   std::vector<LP> Z;
-  if (mode == MODE_DELTA || mode == MODE_DELTA_FE) Z = delta_orbit(*v);
+  if (mode == MODE_DELTA || mode == MODE_DELTA_FE || mode == MODE_DELTA_SINGLE)
+    Z = delta_orbit(*v);
   for (long k = 0; k < npix; k++)
     if (rows[k] < 0 || rows[k] >= v->nr || cols[k] < 0 || cols[k] >= v->nc) return 5;
   parallel_for((size_t)npix, threads, [&](size_t k) {
@@ -918,6 +924,7 @@ int nmo_render_pixels(nmo_view* h, int mode, long npix, const int32_t* rows, con
     if (hw) p = get_iterations_hw(*v, pr, pi, *s);
     else if (mode == MODE_REF) p = get_iterations(*v, pr, pi, *s);
     else if (mode == MODE_DELTA) p = get_iterations_delta(*v, pr, pi, *s, Z);
+    else if (mode == MODE_DELTA_SINGLE) p = get_iterations_delta(*v, pr, pi, *s, Z, false);
     else if (mode == MODE_REF_FE) p = get_iterations_fx(*v, pr, pi, *s);
     else p = get_iterations_delta_fx(*v, pr, pi, *s, Z);
     iters[k] = p.iterations;

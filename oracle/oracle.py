@@ -15,6 +15,7 @@ MODE_REF = 0
 MODE_DELTA = 1
 MODE_REF_FE = 2
 MODE_DELTA_FE = 3
+MODE_DELTA_SINGLE = 4  # planted mistake: no rebase on |Y| < |delta|
 
 _lib = None
 

@@ -1,0 +1,67 @@
+"""Pauldelbrot glitches: views where single-reference perturbation loses
+precision, and what the library's rebasing does there.
+
+The views are two steps of the seeded boundary-following walk (widths 1e-16
+and 1e-40) with the reference orbit at the view center.  There, perturbation
+against that one orbit (the oracle's MODE_DELTA_SINGLE, a planted mistake:
+no rebase when |Y| < |delta|) misses the reference's escape counts on 11-17 %
+of the samples, in connected blobs -- the glitches, where a sample's orbit
+passes far closer to 0 than the reference's.  The GPU's FP64 and FE32 paths
+rebase (Zhuoran) instead: against the reference's own arithmetic on the same
+view (NM_PATH_MP, bit-exact with the oracle's MODE_REF), their misses are
+isolated samples where the view is chaotic at the sample scale, never a blob.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+WALK = json.load(open(os.path.join(HERE, "golden", "deep_centers.json")))["steps"]
+
+
+@pytest.fixture(scope="module")
+def nm():
+    import newman_gb300
+    newman_gb300.load_library()
+    return newman_gb300
+
+
+def _largest_blob(mask):
+    ndimage = pytest.importorskip("scipy.ndimage")
+    lab, n = ndimage.label(mask)
+    return int(np.bincount(lab.ravel())[1:].max()) if n else 0
+
+
+@pytest.mark.parametrize("k", [2, 7])
+def test_rebasing_leaves_no_glitch(nm, oracle_mod, k):
+    from decimal import Decimal, getcontext
+    getcontext().prec = 200
+    n, N = 96, 60000
+    cre, cim = WALK[k - 1]["next_center_re"], WALK[k - 1]["next_center_im"]
+    step = str(Decimal(WALK[k]["width"]) / n)
+    grids = {}
+    for path in ("PATH_MP", "PATH_FP64", "PATH_FE32"):
+        m = nm.Mandelbrot(n, n)
+        m.set_view(cre, cim, step, step, N)
+        m.set_path(getattr(nm, path))
+        m.set_option(nm.OPT_REFERENCE, nm.REFERENCE_CENTER)
+        m.precompute()
+        m.render()
+        grids[path] = m.grid()["iterations"]
+    ref = grids["PATH_MP"]
+    o = oracle_mod.OracleView(n, n)
+    o.set_view(cre, cim, step, step, N)
+    o.precompute(center=True)
+    it_ref, _ = o.render_rows(0, n, oracle_mod.MODE_REF)
+    assert np.array_equal(ref, it_ref)  # the comparator is the reference's arithmetic
+    it_single, _ = o.render_rows(0, n, oracle_mod.MODE_DELTA_SINGLE)
+    single_bad = it_single != ref
+    assert single_bad.mean() > 0.1 and _largest_blob(single_bad) >= 20  # the view glitches
+    for path in ("PATH_FP64", "PATH_FE32"):
+        bad = grids[path] != ref
+        assert bad.mean() <= 0.01, (path, bad.mean())
+        assert _largest_blob(bad) <= 3, path

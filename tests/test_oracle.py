@@ -146,3 +146,33 @@ def test_unbounded_exponent_delta_equals_plain_fp64_in_range(oracle_mod):
     it_x, sm_x = o.render_rows(0, nr, oracle_mod.MODE_DELTA_FE)
     assert np.array_equal(it_d, it_x)
     assert np.array_equal(sm_d, sm_x)
+
+
+def test_rebasing_removes_single_reference_glitches(oracle_mod):
+    """On the seeded walk's view at width 1e-16 with the orbit at the view
+    center, single-reference perturbation (MODE_DELTA_SINGLE, no rebase on
+    |Y| < |delta|) misses the reference's escape counts in connected blobs
+    (Pauldelbrot's glitches); the library's rebasing perturbation (MODE_DELTA)
+    misses only isolated chaotic samples."""
+    import json
+    import os
+    from decimal import Decimal, getcontext
+    ndimage = pytest.importorskip("scipy.ndimage")
+    walk = json.load(open(os.path.join(os.path.dirname(__file__), "golden",
+                                       "deep_centers.json")))["steps"]
+    getcontext().prec = 200
+    n = 48
+    step = str(Decimal(walk[2]["width"]) / n)
+    o = oracle_mod.OracleView(n, n)
+    o.set_view(walk[1]["next_center_re"], walk[1]["next_center_im"], step, step, 60000)
+    o.precompute(center=True)
+    ref, _ = o.render_rows(0, n, oracle_mod.MODE_REF)
+
+    def largest(mask):
+        lab, k = ndimage.label(mask)
+        return int(np.bincount(lab.ravel())[1:].max()) if k else 0
+
+    single, _ = o.render_rows(0, n, oracle_mod.MODE_DELTA_SINGLE)
+    rebased, _ = o.render_rows(0, n, oracle_mod.MODE_DELTA)
+    assert (single != ref).mean() > 0.05 and largest(single != ref) >= 10
+    assert (rebased != ref).mean() < 0.02 and largest(rebased != ref) <= 3

@@ -418,7 +418,7 @@ def run_ours(args):
         # (same center and sample step, fewer samples): the case the ncu
         # captures run on.
         NR, NC = NR // args.profile, NC // args.profile
-        for path in (nm.PATH_FE32, nm.PATH_FP64):
+        for path in (nm.PATH_FE32, nm.PATH_FP64, nm.PATH_MP):
             mm = make(path)
             mm.precompute()
             mm.render()

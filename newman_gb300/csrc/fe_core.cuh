@@ -402,8 +402,8 @@ __device__ __forceinline__ bool fe_scaled_steps(const DeviceView& v, FeState& st
   for (; st.i < stop; st.i++) {
     const FF sd_r = st.E < -140 ? FF{0.f, 0.f} : ff_scale(st.dr, st.E);
     const FF sd_i = st.E < -140 ? FF{0.f, 0.f} : ff_scale(st.di, st.E);
-    const FF tr = ff_add(FF{2.0f * z.hx, 2.0f * z.lx}, sd_r);
-    const FF ti = ff_add(FF{2.0f * z.hy, 2.0f * z.ly}, sd_i);
+    const FF tr = ff_add_twice(z.hx, z.lx, sd_r);
+    const FF ti = ff_add_twice(z.hy, z.ly, sd_i);
     const float zl1 = up_add(fabsf(z.hx), fabsf(z.hy)), dl1 = up_add(fabsf(st.dr.h), fabsf(st.di.h));
     FF nr, ni;
     ff_cmul_add(tr, ti, st.dr, st.di, st.er, st.ei, nr, ni);
@@ -507,8 +507,8 @@ __device__ __forceinline__ bool fe_unscaled_steps(const DeviceView& v, FeState& 
   float ym = approx_norm(z.hx + dr.h, z.hy + di.h);
   bool done = false;
   for (; i < stop; i++) {
-    const FF tr = ff_add(FF{2.0f * z.hx, 2.0f * z.lx}, dr);
-    const FF ti = ff_add(FF{2.0f * z.hy, 2.0f * z.ly}, di);
+    const FF tr = ff_add_twice(z.hx, z.lx, dr);
+    const FF ti = ff_add_twice(z.hy, z.ly, di);
     const float zl1 = up_add(fabsf(z.hx), fabsf(z.hy)), dl1 = up_add(fabsf(dr.h), fabsf(di.h));
     const float ym_up = up_fma(0x1p-20f, up_add(zl1, dl1), ym);
     const float loc = up_fma(kFeUT, up_mul(up_fma(2.0f, zl1, dl1), dl1), ueps);

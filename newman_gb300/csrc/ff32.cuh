@@ -39,6 +39,15 @@ NM_HD FF ff_add(FF a, FF b) {
   const FF s = ff_two_sum(a.h, b.h);
   return ff_fast_two_sum(s.h, fadd_(s.l, fadd_(a.l, b.l)));
 }
+// ff_add({2 a.h, 2 a.l}, b) with the doubling folded into fused multiply-adds:
+// 2x is exact in floats, so fma(2, x, y) = RN(2x + y) = RN(RN(2x) + y) and
+// every value below is the same bits as ff_add's on the doubled operand.
+NM_HD FF ff_add_twice(float ah, float al, FF b) {
+  const float s = ffma_(2.0f, ah, b.h);           // fadd_(2 ah, b.h)
+  const float bb = ffma_(-2.0f, ah, s);           // fsub_(s, 2 ah)
+  const float e = fadd_(ffma_(2.0f, ah, -fsub_(s, bb)), fsub_(b.h, bb));
+  return ff_fast_two_sum(s, fadd_(e, ffma_(2.0f, al, b.l)));
+}
 NM_HD FF ff_from_double(double x) {
   const float h = (float)x;
   return {h, (float)(x - (double)h)};

@@ -328,8 +328,15 @@ __device__ __forceinline__ bool fe_front_start(const DeviceView& v, int r, int c
 
 // sqrt(x) from the hardware reciprocal square root (relative error below
 // 2^-21; 0 for x = 0).
+// sqrt(x) from the hardware reciprocal square root (relative error below
+// 2^-22.9; with the product's rounding within 2^-21).  Below x = 2^-120 the
+// result is 2^-60, above sqrt(x): the FE32 step only uses the estimate of |Y|
+// as an upper bound (its error amplification, the bailout gap 1024 - |Y|),
+// and the flush-to-zero form needs no subnormal handling.
 __device__ __forceinline__ float approx_sqrt(float x) {
-  return x > 0.0f ? x * rsqrtf(x) : 0.0f;
+  float r;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return x > 0x1p-120f ? x * r : 0x1p-60f;
 }
 __device__ __forceinline__ float approx_norm(float x, float y) {
   return approx_sqrt(fmaf(x, x, y * y));

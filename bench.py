@@ -422,9 +422,9 @@ def run_ours(args):
             mm = make(path)
             mm.precompute()
             mm.render()
-            print("profile case %dx%d samples, path %d: %.1f ms, rework %d" % (
+            print("profile case %dx%d samples, path %d: %.1f ms, rework %d, executed steps %d" % (
                 mm.rows(), mm.cols(), path, mm.stat(nm.STAT_KERNEL_NS) * 1e-6,
-                mm.stat(nm.STAT_FP64_REWORK)))
+                mm.stat(nm.STAT_FP64_REWORK), mm.stat(nm.STAT_EXECUTED_ITERS)))
         return
     m = make(primary)
     t0 = time.perf_counter()

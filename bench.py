@@ -353,6 +353,8 @@ def apply_orbit_options(nm, m, args):
         m.set_option(nm.OPT_ORBIT_STAGE, args.orbit_stage)
     if getattr(args, "l2_window", None) is not None:
         m.set_option(nm.OPT_L2_WINDOW, args.l2_window)
+    if getattr(args, "fe32_overlap", None) is not None:
+        m.set_option(nm.OPT_FE32_OVERLAP, args.fe32_overlap)
 
 
 def torch_stream(stream):
@@ -1030,6 +1032,8 @@ def main():
                     help="rows: one C2 view split by rows across the ranks (strong scaling)")
     ap.add_argument("--orbit-stage", type=int, default=None,
                     help="FE32: orbit entries staged in shared memory (NM_OPT_ORBIT_STAGE)")
+    ap.add_argument("--fe32-overlap", type=int, default=None,
+                    help="FE32: 0 = the FP64 rework after the iteration pass (NM_OPT_FE32_OVERLAP)")
     ap.add_argument("--l2-window", type=int, default=None,
                     help="FE32: 1 = persisting L2 window on the orbit (NM_OPT_L2_WINDOW)")
     ap.add_argument("--autotune", action="store_true")

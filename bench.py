@@ -139,7 +139,9 @@ def max_over_ranks(ms, device=None):
     return float(t.item())
 
 
-INSTR_PER_ITER = 128.7  # FE32 step: 5.30e12 thread instructions for 4.12e10 steps (ncu)
+# FE32 step: 1.411e12 thread instructions for 1.209e10 steps, the iteration
+# kernel alone (--fe32-overlap 0) on the central 540x960-pixel crop (ncu)
+INSTR_PER_ITER = 116.7
 
 
 def issue_roofline(executed, iter_ms, clocks):

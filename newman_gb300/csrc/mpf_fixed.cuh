@@ -73,22 +73,49 @@ MPF_HD int clz64(uint64_t x) {
 #endif
 }
 
-// a + b + c (c in {0, 1}); c becomes the carry out.
+// a + b + c (c in {0, 1}); c becomes the carry out.  On the GPU through the
+// hardware carry flag: c sets it (c + 2^64 - 1 carries exactly when c = 1).
 MPF_HD uint64_t addc(uint64_t a, uint64_t b, uint64_t& c) {
+#if defined(__CUDA_ARCH__)
+  uint64_t r;
+  asm volatile(
+      "{\n\t.reg .u64 t;\n\t"
+      "add.cc.u64 t, %2, 0xffffffffffffffff;\n\t"
+      "addc.cc.u64 %0, %3, %4;\n\t"
+      "addc.u64 %1, 0, 0;\n\t}"
+      : "=l"(r), "=l"(c)
+      : "l"(c), "l"(a), "l"(b));
+  return r;
+#else
   const uint64_t t = a + b;
   const uint64_t c1 = t < a;
   const uint64_t u = t + c;
   c = c1 | (uint64_t)(u < t);
   return u;
+#endif
 }
 
-// a - b - br (br in {0, 1}); br becomes the borrow out.
+// a - b - br (br in {0, 1}); br becomes the borrow out.  On the GPU through
+// the hardware borrow flag: 0 - br borrows exactly when br = 1.
 MPF_HD uint64_t subb(uint64_t a, uint64_t b, uint64_t& br) {
+#if defined(__CUDA_ARCH__)
+  uint64_t r, bo;
+  asm volatile(
+      "{\n\t.reg .u64 t;\n\t"
+      "sub.cc.u64 t, 0, %2;\n\t"
+      "subc.cc.u64 %0, %3, %4;\n\t"
+      "subc.u64 %1, 0, 0;\n\t}"
+      : "=l"(r), "=l"(bo)
+      : "l"(br), "l"(a), "l"(b));
+  br = bo ? 1 : 0;  // the borrow out comes as 0 or 2^64 - 1
+  return r;
+#else
   const uint64_t t = a - b;
   const uint64_t b1 = a < b;
   const uint64_t u = t - br;
   br = b1 | (uint64_t)(t < br);
   return u;
+#endif
 }
 
 // d[k] for a runtime k, 0 outside [0, D): on the GPU by selects over the
@@ -153,6 +180,29 @@ MPF_HD Mpfx<P> mpf_mul(const Mpfx<P>& a, const Mpfx<P>& b) {
   uint64_t r[2 * P];
 #pragma unroll
   for (int k = 0; k < 2 * P; k++) r[k] = 0;
+#if defined(__CUDA_ARCH__)
+  // row i: r[i .. i+P] += a_i * b, the low halves of the products in one
+  // carry chain, their high halves in a second (the row's sum fits: the
+  // final carry is 0)
+#pragma unroll
+  for (int i = 0; i < P; i++) {
+    const uint64_t ai = a.d[P - 1 - i];
+    asm volatile("mad.lo.cc.u64 %0, %1, %2, %0;" : "+l"(r[i]) : "l"(ai), "l"(b.d[P - 1]));
+#pragma unroll
+    for (int j = 1; j < P; j++)
+      asm volatile("madc.lo.cc.u64 %0, %1, %2, %0;"
+                   : "+l"(r[i + j])
+                   : "l"(ai), "l"(b.d[P - 1 - j]));
+    asm volatile("addc.u64 %0, 0, 0;" : "=l"(r[i + P]));
+    asm volatile("mad.hi.cc.u64 %0, %1, %2, %0;" : "+l"(r[i + 1]) : "l"(ai), "l"(b.d[P - 1]));
+#pragma unroll
+    for (int j = 1; j < P - 1; j++)
+      asm volatile("madc.hi.cc.u64 %0, %1, %2, %0;"
+                   : "+l"(r[i + 1 + j])
+                   : "l"(ai), "l"(b.d[P - 1 - j]));
+    asm volatile("madc.hi.u64 %0, %1, %2, %0;" : "+l"(r[i + P]) : "l"(ai), "l"(b.d[0]));
+  }
+#else
 #pragma unroll
   for (int i = 0; i < P; i++) {
     const uint64_t ai = a.d[P - 1 - i];
@@ -172,6 +222,7 @@ MPF_HD Mpfx<P> mpf_mul(const Mpfx<P>& a, const Mpfx<P>& b) {
     }
     r[i + P] = carry;
   }
+#endif
   // top limb zero: one limb lower
   const bool adj = r[2 * P - 1] == 0;
   Mpfx<P> o;

@@ -513,35 +513,18 @@ __device__ __forceinline__ bool fe_unscaled_steps(const DeviceView& v, FeState& 
   // own error (2^-22)
   float ym = approx_norm(z.hx + dr.h, z.hy + di.h);
   bool done = false;
-#if defined(__CUDA_ARCH__)
-  const FF2 epsp{f2_pack(er.h, ei.h), f2_pack(er.l, ei.l)};
-#endif
   for (; i < stop; i++) {
-#if defined(__CUDA_ARCH__)
-    // t = 2Z + delta and delta' = t delta + eps with the real and imaginary
-    // parts in one packed FP32x2 instruction each (ff32.cuh): the same bits
-    // as ff_add_twice and ff_cmul_add
-    const FF2 dp{f2_pack(dr.h, di.h), f2_pack(dr.l, di.l)};
-    const FF2 tp = ff2_add_twice(f2_pack(z.hx, z.hy), f2_pack(z.lx, z.ly), dp);
-#else
     const FF tr = ff_add_twice(z.hx, z.lx, dr);
     const FF ti = ff_add_twice(z.hy, z.ly, di);
-#endif
     const float zl1 = up_add(fabsf(z.hx), fabsf(z.hy)), dl1 = up_add(fabsf(dr.h), fabsf(di.h));
     const float ym_up = up_fma(0x1p-20f, up_add(zl1, dl1), ym);
     const float loc = up_fma(kFeUT, up_mul(up_fma(2.0f, zl1, dl1), dl1), ueps);
     const float err_old = err;
     err = up_fma(up_fma(2.0f, ym_up, err), err, loc);  // 2|Y| e + e^2 + local rounding
-#if defined(__CUDA_ARCH__)
-    const FF2 np = ff2_cmul_add(tp, dp, epsp);
-    dr = FF{f2_x(np.h), f2_x(np.l)};
-    di = FF{f2_y(np.h), f2_y(np.l)};
-#else
     FF nr, ni;
     ff_cmul_add(tr, ti, dr, di, er, ei, nr, ni);
     dr = nr;
     di = ni;
-#endif
     j++;
     z = fe_load_z<kStaged>(v, j);
     const float yr = z.hx + dr.h, yi = z.hy + di.h;

@@ -345,6 +345,7 @@ def c3_deep(nm, steps, flush, stream, args=None):
             "executed_iters": executed, "effective_iters": eff,
             "executed_iters_per_s": executed / (fe_ms * 1e-3),
             "fp64_rework_samples": rework, "wait_timeouts": timeouts,
+            "cardioid_undecided": m.stat(nm.STAT_CARDIOID_UNDECIDED),
             "interior_fraction": float((g["iterations"] == N).mean())}
 
 
@@ -474,6 +475,7 @@ def run_ours(args):
     rework = m.stat(nm.STAT_FP64_REWORK)
     front_fp64 = m.stat(nm.STAT_FRONT_FP64)
     timeouts = m.stat(nm.STAT_WAIT_TIMEOUTS)
+    undecided = m.stat(nm.STAT_CARDIOID_UNDECIDED)
     k_main_ms = m.stat(nm.STAT_KERNEL_NS) * 1e-6
     k_rework_ms = m.stat(nm.STAT_REWORK_KERNEL_NS) * 1e-6
     k_iter_ms = m.stat(nm.STAT_ITER_KERNEL_NS) * 1e-6
@@ -553,7 +555,7 @@ def run_ours(args):
                           "fp64_rework": k_rework_ms},
             "executed_iters_per_step": executed, "effective_iters_per_step": eff_iters,
             "executed_iters_per_s": executed / (ms * 1e-3),
-            "wait_timeouts": timeouts,
+            "wait_timeouts": timeouts, "cardioid_undecided": undecided,
             "precompute_s": precompute_s, "wall_s": wall,
             # kernels the library launched during the timed steps (its own count)
             "gpu_launches": launches,

@@ -266,7 +266,8 @@ int nm_cost_model_train(nm_costmodel* m, const float* features, const float* tar
    render replays it.  Frames must be precomputed first and stay alive while
    in the batch; a frame whose tables or grid change is noticed and the graph
    rebuilt.  sc: the frames' multisample factor (their rows and columns are
-   multiples of it); nm_batch_frames returns the reduced frames, frame-major. */
+   multiples of it); nm_batch_frames returns the reduced frames, frame-major.
+   Frames on NM_PATH_MP are refused (NM_ERR_UNSUPPORTED): render them alone. */
 typedef struct nm_batch nm_batch;
 nm_batch* nm_batch_create(int sc);
 void nm_batch_destroy(nm_batch* b);

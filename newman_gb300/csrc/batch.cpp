@@ -116,6 +116,9 @@ int build(nm_batch* b) {
     nmg::DeviceView v;
     nmg::KernelKind kind;
     if (int rc = nmg::prepare_view(h, 0, h->view.rows(), v, kind)) return rc;
+    if (kind == nmg::KERNEL_MP || kind == nmg::KERNEL_HW_MP)
+      return fail(NM_ERR_UNSUPPORTED, "a batch renders the FE32, FP64 and double-loop paths; "
+                                      "render reference-exact frames alone");
     if (kind == nmg::KERNEL_FE32) {
       fe.push_back(v);
       off_fe.push_back(off_fe.back() + v.total);
@@ -247,6 +250,9 @@ void nm_batch_destroy(nm_batch* b) {
 
 int nm_batch_add(nm_batch* b, nm_handle* frame) {
   if (!b || !frame) return fail(NM_ERR_ARG, "null batch or frame");
+  if (frame->path == NM_PATH_MP)
+    return fail(NM_ERR_UNSUPPORTED, "a batch renders the FE32, FP64 and double-loop paths; "
+                                    "render reference-exact frames alone");
   if (frame->view.rows() % b->sc || frame->view.cols() % b->sc)
     return fail(NM_ERR_ARG, "frame %d x %d is not a multiple of the multisample factor %d",
                 frame->view.rows(), frame->view.cols(), b->sc);

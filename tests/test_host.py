@@ -175,3 +175,15 @@ def test_render_without_gpu_fails_loudly():
     with pytest.raises(nm.NewmanError) as e:
         m.render()
     assert e.value.code == nm.NM_ERR_CUDA
+
+
+def test_batch_refuses_reference_exact_frames():
+    """A batch groups its frames by the FE32, FP64 and double-loop kernels;
+    a frame on the reference-exact path is refused, not rendered by another
+    path's arithmetic (host check: the refusal comes before any GPU work)."""
+    m = nm.Mandelbrot(8, 8)
+    m.set_path(nm.PATH_MP)
+    b = nm.Batch(sc=1)
+    with pytest.raises(nm.NewmanError) as e:
+        b.add(m)
+    assert e.value.code == nm.NM_ERR_UNSUPPORTED

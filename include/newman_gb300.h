@@ -85,9 +85,12 @@ enum nm_option {
                                copied into each block's shared memory by the TMA unit, where
                                every rebased sample restarts (0: none; -1, the default: 1024 on
                                views whose series leaves the double range, else none) */
-  NM_OPT_L2_WINDOW = 14     /* FE32 iteration pass: 1 runs it with a persisting L2 access-policy
+  NM_OPT_L2_WINDOW = 14,    /* FE32 iteration pass: 1 runs it with a persisting L2 access-policy
                                window over the reference orbit (the process's L2 set-aside is
                                raised to the orbit's size, within the device's limit) */
+  NM_OPT_ITER_CAP = 15      /* renders stop every sample at min(N, cap) iterations (0: N), as
+                               if N were the cap: for previews that show where a view's work
+                               lies without running its longest samples to the end */
 };
 
 enum nm_stat {
@@ -119,7 +122,9 @@ nm_handle* nm_copy(const nm_handle* src);
 /* No reference counterpart: the same view on a grid `factor` times coarser in
    each direction (rows and columns must be multiples of it).  A precomputed
    view with its reference orbit at the view center shares that orbit and its
-   series: the preview is ready to render without nm_precompute. */
+   series: the preview is ready to render without nm_precompute, and reads the
+   source's orbit and series tables in place (host and GPU; the first render
+   of either uploads them) -- destroy the preview before its source. */
 nm_handle* nm_preview(const nm_handle* src, int factor);
 void nm_destroy(nm_handle* h);
 const char* nm_last_error(void);

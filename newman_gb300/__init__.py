@@ -21,7 +21,7 @@ NM_OK, NM_ERR_ARG, NM_ERR_PARSE, NM_ERR_STATE, NM_ERR_CUDA, NM_ERR_CANCELLED, NM
 PATH_REFERENCE, PATH_FP64, PATH_FE32, PATH_MP = 0, 1, 2, 3
 OPT_TILE_W, OPT_TILE_H, OPT_CHUNK, OPT_KEEP_SMOOTH64, OPT_THREADS, OPT_BLOCKS, OPT_RENORM, \
     OPT_FE32_SINGLE_PASS, OPT_REFERENCE, OPT_BATCH_GRAPH, OPT_FE32_OVERLAP, \
-    OPT_LOG_TILE_COSTS, OPT_BATCH_FP64_WARPS, OPT_ORBIT_STAGE, OPT_L2_WINDOW = range(15)
+    OPT_LOG_TILE_COSTS, OPT_BATCH_FP64_WARPS, OPT_ORBIT_STAGE, OPT_L2_WINDOW, OPT_ITER_CAP = range(16)
 REFERENCE_PROBES, REFERENCE_CENTER = 0, 1
 STAT_CARDIOID_UNDECIDED, STAT_EXECUTED_ITERS, STAT_SAMPLES, STAT_REBASES, STAT_FP64_REWORK, \
     STAT_WAIT_TIMEOUTS, STAT_FRONT_FP64, STAT_STAGE_FALLBACKS = range(8)
@@ -334,12 +334,15 @@ class Mandelbrot:
 
     # ---- learned tile scheduling (no reference counterpart) -----------------
     def preview(self, factor):
-        """The same view on a grid `factor` times coarser (nm_preview); shares a
-        precomputed view-center orbit."""
+        """The same view on a grid `factor` times coarser (nm_preview); reads a
+        precomputed view-center orbit and series in place, so it renders only
+        while this view keeps them (a new precompute or view makes it refuse)."""
         h = _lib.nm_preview(self._h, int(factor))
         if not h:
             raise NewmanError(NM_ERR_ARG, _lib.nm_last_error().decode())
-        return Mandelbrot(_handle=h)
+        p = Mandelbrot(_handle=h)
+        p._source = self  # the preview may read this view's orbit in place
+        return p
 
     def tiles(self):
         """(tiles_x, tiles_y) of the whole grid at the current tile size."""

@@ -141,7 +141,7 @@ int build(nm_batch* b) {
     }
     b->seen_gen.push_back(h->generation);
     b->seen_grid.push_back(h->grid.p);
-    b->seen_orbit.push_back(h->d_zf.p);
+    b->seen_orbit.push_back(h->tables()->d_zf.p);
   }
   if (off_fe.back() > 0xffffffffll)
     return fail(NM_ERR_ARG, "batch of %lld FE32 samples exceeds 2^32", off_fe.back());
@@ -222,8 +222,8 @@ bool stale(const nm_batch* b) {
   if (!b->built || b->seen_grid.size() != b->frames.size()) return true;
   for (size_t k = 0; k < b->frames.size(); k++) {
     const nm_handle* h = b->frames[k];
-    if (!h->uploaded || h->generation != b->seen_gen[k] || h->grid.p != b->seen_grid[k] ||
-        h->d_zf.p != b->seen_orbit[k])
+    if (!h->uploaded || h->tables_stale() || h->generation != b->seen_gen[k] ||
+        h->grid.p != b->seen_grid[k] || h->tables()->d_zf.p != b->seen_orbit[k])
       return true;
   }
   return false;

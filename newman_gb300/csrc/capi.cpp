@@ -148,16 +148,23 @@ int do_upload(nm_handle* h) {
     if ((rc = upload(h->d_coord_re_mp, h->coord_re_mp, h->stream))) return rc;
     if ((rc = upload(h->d_coord_im_mp, h->coord_im_mp, h->stream))) return rc;
   }
-  if (h->precomputed && !h->od.xmp.empty())
+  // a sharing preview reads its source's orbit and series (uploaded there)
+  if (h->tables_stale()) return fail(NM_ERR_STATE, kStalePreview);
+  if (h->orbit_src && !h->orbit_src->uploaded)
+    if ((rc = do_upload(h->orbit_src))) return rc;
+  const bool own = h->orbit_src == nullptr;
+  if (own && h->precomputed && !h->od.xmp.empty())
     if ((rc = upload(h->d_x_mp, h->od.xmp, h->stream))) return rc;
   if (h->precomputed) {
+    if ((rc = upload(h->d_eps_re, h->eps_re, h->stream))) return rc;
+    if ((rc = upload(h->d_eps_im, h->eps_im, h->stream))) return rc;
+  }
+  if (h->precomputed && own) {
     auto cv = [](const std::vector<nmg::D2>& v) {
       std::vector<Dbl2> o(v.size());
       std::memcpy(o.data(), v.data(), v.size() * sizeof(Dbl2));
       return o;
     };
-    if ((rc = upload(h->d_eps_re, h->eps_re, h->stream))) return rc;
-    if ((rc = upload(h->d_eps_im, h->eps_im, h->stream))) return rc;
     const size_t zlen = h->od.z.size();
     std::vector<nmg::Flt4> zf(2 * zlen);
     for (size_t k = 0; k < zlen; k++) {
@@ -174,21 +181,25 @@ int do_upload(nm_handle* h) {
     if ((rc = upload(h->d_c, cv(h->od.c), h->stream))) return rc;
     if ((rc = upload(h->d_sa_min, h->od.sa_min, h->stream))) return rc;
     if (!h->od.double_loop) {
-      if ((rc = upload(h->d_eps32_re, h->eps32_re, h->stream))) return rc;
-      if ((rc = upload(h->d_eps32_im, h->eps32_im, h->stream))) return rc;
       if ((rc = upload(h->d_a32, h->a32, h->stream))) return rc;
       if ((rc = upload(h->d_b32, h->b32, h->stream))) return rc;
       if ((rc = upload(h->d_c32, h->c32, h->stream))) return rc;
       if ((rc = upload(h->d_sa_min32, h->sa_min32, h->stream))) return rc;
     }
     if (!h->od.sa_fp64_ok) {
-      if ((rc = upload(h->d_eps_re_fe, h->eps_re_fe, h->stream))) return rc;
-      if ((rc = upload(h->d_eps_im_fe, h->eps_im_fe, h->stream))) return rc;
       if ((rc = upload(h->d_a_fe, h->od.a_fe, h->stream))) return rc;
       if ((rc = upload(h->d_b_fe, h->od.b_fe, h->stream))) return rc;
       if ((rc = upload(h->d_c_fe, h->od.c_fe, h->stream))) return rc;
       if ((rc = upload(h->d_sa_min_fe, h->od.sa_min_fe, h->stream))) return rc;
     }
+  }
+  if (h->precomputed && !h->od.double_loop) {  // per row / column, every handle its own
+    if ((rc = upload(h->d_eps32_re, h->eps32_re, h->stream))) return rc;
+    if ((rc = upload(h->d_eps32_im, h->eps32_im, h->stream))) return rc;
+  }
+  if (h->precomputed && !h->od.sa_fp64_ok) {
+    if ((rc = upload(h->d_eps_re_fe, h->eps_re_fe, h->stream))) return rc;
+    if ((rc = upload(h->d_eps_im_fe, h->eps_im_fe, h->stream))) return rc;
   }
   // The vectors above are pageable; the copies are complete when the stream
   // reaches this point, so wait before the host may touch them again.
@@ -228,9 +239,9 @@ nmg::TFE tfe_of(double m, int e) {
 
 // The series front's values in float-float with int exponents: eps per
 // column / row, A, B, C and the thresholds per index.  Deep views only.
-void build_front32_tables(nm_handle* h) {
+void build_front32_tables(nm_handle* h, bool series = true) {
   const nmg::OrbitData& od = h->od;
-  const int n = od.xlen;
+  const int n = series ? od.xlen : 0;
   h->a32.resize(n);
   h->b32.resize(n);
   h->c32.resize(n);
@@ -269,23 +280,24 @@ int check_handle(const nm_handle* h) {
 
 // Views outside the FP64 range run their series front in floatexp.
 void set_fe_tables(const nm_handle* h, nmg::DeviceView& v) {
+  const nm_handle* t = h->tables();  // the orbit and series (a sharing preview: its source's)
   v.sa_scan = 0;
-  if (!h->od.double_loop && !h->a32.empty()) {
+  if (!h->od.double_loop && !t->a32.empty()) {
     v.eps32_re = h->d_eps32_re.p;
     v.eps32_im = h->d_eps32_im.p;
-    v.sa_a32 = h->d_a32.p;
-    v.sa_b32 = h->d_b32.p;
-    v.sa_c32 = h->d_c32.p;
-    v.sa_min32 = h->d_sa_min32.p;
+    v.sa_a32 = t->d_a32.p;
+    v.sa_b32 = t->d_b32.p;
+    v.sa_c32 = t->d_c32.p;
+    v.sa_min32 = t->d_sa_min32.p;
   }
   v.sa_fe = h->od.sa_fp64_ok ? 0 : 1;
   if (!v.sa_fe) return;
   v.eps_re_fe = h->d_eps_re_fe.p;
   v.eps_im_fe = h->d_eps_im_fe.p;
-  v.sa_a_fe = h->d_a_fe.p;
-  v.sa_b_fe = h->d_b_fe.p;
-  v.sa_c_fe = h->d_c_fe.p;
-  v.sa_min_fe = h->d_sa_min_fe.p;
+  v.sa_a_fe = t->d_a_fe.p;
+  v.sa_b_fe = t->d_b_fe.p;
+  v.sa_c_fe = t->d_c_fe.p;
+  v.sa_min_fe = t->d_sa_min_fe.p;
 }
 
 }  // namespace
@@ -295,6 +307,7 @@ int nmg::prepare_view(nm_handle* h, int r0, int r1, nmg::DeviceView& v, nmg::Ker
   const bool hw = h->view.use_hardware() &&
                   (h->path == NM_PATH_REFERENCE || h->path == NM_PATH_MP || double_loop_direct(h));
   const int mp_limbs = nmg::mp_limbs_for_bits(h->view.bits());
+  if (h->tables_stale()) return fail(NM_ERR_STATE, kStalePreview);
   if (h->path == NM_PATH_MP) {
     if (mp_limbs < nmg::kMpMinLimbs || mp_limbs > nmg::kMpMaxLimbs)
       return fail(NM_ERR_UNSUPPORTED, "the reference-exact path takes 64 to %d bits of precision "
@@ -318,7 +331,7 @@ int nmg::prepare_view(nm_handle* h, int r0, int r1, nmg::DeviceView& v, nmg::Ker
   std::memset(&v, 0, sizeof v);
   v.nr = nr;
   v.nc = nc;
-  v.N = h->view.iterations();
+  v.N = h->effective_N();
   v.cardioid_mode = h->outside_cardioid ? nmg::CARDIOID_NONE : nmg::CARDIOID_PER_SAMPLE;
   v.tol = h->view.tolerance();
   v.bailout2 = 1024.0 * 1024.0;
@@ -334,18 +347,19 @@ int nmg::prepare_view(nm_handle* h, int r0, int r1, nmg::DeviceView& v, nmg::Ker
   v.coord_im = h->d_coord_im.p;
   v.c_abs = coord_abs_bound(h);
   if (!hw) {
+    const nm_handle* t = h->tables();  // a sharing preview: its source's orbit and series
     v.eps_re = h->d_eps_re.p;
     v.eps_im = h->d_eps_im.p;
-    v.z = h->orbit_z();
-    v.zf = h->d_zf.p;
-    v.zlen = (int)h->od.z.size();
+    v.z = t->orbit_z();
+    v.zf = t->d_zf.p;
+    v.zlen = (int)t->zlen();
     v.xlen = h->od.xlen;
-    v.xhi = h->d_xhi.p;
-    v.xlo = h->d_xlo.p;
-    v.sa_a = h->d_a.p;
-    v.sa_b = h->d_b.p;
-    v.sa_c = h->d_c.p;
-    v.sa_min = h->d_sa_min.p;
+    v.xhi = t->d_xhi.p;
+    v.xlo = t->d_xlo.p;
+    v.sa_a = t->d_a.p;
+    v.sa_b = t->d_b.p;
+    v.sa_c = t->d_c.p;
+    v.sa_min = t->d_sa_min.p;
     set_fe_tables(h, v);
     v.double_loop = h->od.double_loop ? 1 : 0;
     if (h->od.double_loop) {  // the FE32 path on a double-loop view: trapping records
@@ -370,7 +384,7 @@ int nmg::prepare_view(nm_handle* h, int r0, int r1, nmg::DeviceView& v, nmg::Ker
     v.mp_limbs = mp_limbs;
     v.coord_re_mp = h->d_coord_re_mp.p;
     v.coord_im_mp = h->d_coord_im_mp.p;
-    v.x_mp = hw ? nullptr : h->d_x_mp.p;
+    v.x_mp = hw ? nullptr : h->tables()->d_x_mp.p;
     kind = hw ? nmg::KERNEL_HW_MP : nmg::KERNEL_MP;
     return NM_OK;
   }
@@ -431,6 +445,10 @@ nm_handle* nm_copy(const nm_handle* src) {
   h->tile_order_h = src->tile_order_h;
   h->log_costs = src->log_costs;
   h->od = src->od;
+  h->od_zlen = src->od_zlen;
+  h->orbit_src = src->orbit_src;
+  h->src_stamp = src->src_stamp;
+  h->iter_cap = src->iter_cap;
   h->precomputed = src->precomputed;
   h->coords_valid = src->coords_valid;
   h->outside_cardioid = src->outside_cardioid;
@@ -560,6 +578,10 @@ int nm_set_option(nm_handle* h, int opt, long long value) {
     case NM_OPT_L2_WINDOW:
       h->l2_window = value != 0;
       return NM_OK;
+    case NM_OPT_ITER_CAP:
+      if (value < 0 || value > (1ll << 31) - 1) return fail(NM_ERR_ARG, "iteration cap %lld", value);
+      h->iter_cap = (int)value;
+      return NM_OK;
     case NM_OPT_REFERENCE:
       if (value != nmg::REFERENCE_PROBES && value != nmg::REFERENCE_CENTER)
         return fail(NM_ERR_ARG, "reference mode %lld", value);
@@ -645,6 +667,9 @@ int nm_precompute(nm_handle* h) {
   h->coords_valid = false;
   if (int rc = ensure_coords(h)) return rc;
   h->precomputed = false;
+  h->orbit_src = nullptr;  // from here on the handle's own orbit
+  h->od_zlen = 0;
+  h->tables_stamp++;  // previews sharing the old orbit no longer render
   if (double_loop_direct(h)) {
     // rendered by the double loop: nothing to precompute
   } else if (h->view.use_hardware() && h->path == NM_PATH_FE32) {
@@ -677,6 +702,7 @@ int nm_precompute(nm_handle* h) {
 
 int nm_get_orbit(nm_handle* h, double* x, double* xlo, double* a, double* b, double* c, int n) {
   if (int rc = check_handle(h)) return rc;
+  if (h->orbit_src && h->precomputed) h = h->orbit_src;
   if (!h->precomputed || h->od.double_loop) return fail(NM_ERR_STATE, "no precomputed orbit and series");
   if (n != h->od.xlen) return fail(NM_ERR_ARG, "%d entries for an orbit of %d", n, h->od.xlen);
   for (int i = 0; i < n; i++) {
@@ -920,9 +946,22 @@ nm_handle* nm_preview(const nm_handle* src, int factor) {
       for (size_t r = 0; r < py.size(); r++) py[r] = h->coord_im[r].x;
       h->view.eps_tables_double_loop(px, py, h->eps_re, h->eps_im);
     } else {
+      // the orbit and series stay with their owner, read in place (host
+      // vectors and device tables): only their sizes and flags come along
+      const nm_handle* owner = src->tables();
+      h->orbit_src = const_cast<nm_handle*>(owner);
+      h->src_stamp = owner->tables_stamp;
+      nmg::OrbitData lite;
+      lite.xlen = src->od.xlen;
+      lite.probe_index = src->od.probe_index;
+      lite.sa_fp64_ok = src->od.sa_fp64_ok;
+      lite.double_loop = src->od.double_loop;
+      lite.mp_limbs = src->od.mp_limbs;
+      h->od = std::move(lite);
+      h->od_zlen = owner->zlen();
       h->view.eps_tables(h->od, h->eps_re, h->eps_im);
       if (!h->od.sa_fp64_ok) h->view.eps_tables_fe(h->eps_re_fe, h->eps_im_fe);
-      build_front32_tables(h.get());
+      build_front32_tables(h.get(), /*series=*/false);
     }
     h->precomputed = true;
   }
@@ -1121,7 +1160,12 @@ void noalloc_fail(const std::string& why) { g_last_error = why; }
 // allocation-free entry point (noalloc.cu): only reads the handle.
 int noalloc_view(nm_handle* h, DeviceView& v, int& device, std::string& why, KernelKind& kind) {
   kind = double_loop_direct(h) ? KERNEL_HW : KERNEL_FE32;
-  if (!h->uploaded || !h->stream || (kind == KERNEL_FE32 && (!h->precomputed || !h->d_zf.p))) {
+  if (h->tables_stale()) {
+    why = kStalePreview;
+    return NM_ERR_STATE;
+  }
+  if (!h->uploaded || !h->stream ||
+      (kind == KERNEL_FE32 && (!h->precomputed || !h->tables()->d_zf.p || !h->tables()->uploaded))) {
     why = "the view's tables are not on the GPU: call nm_precompute and nm_upload first";
     return NM_ERR_STATE;
   }
@@ -1129,7 +1173,7 @@ int noalloc_view(nm_handle* h, DeviceView& v, int& device, std::string& why, Ker
   std::memset(&v, 0, sizeof v);
   v.nr = nr;
   v.nc = nc;
-  v.N = h->view.iterations();
+  v.N = h->effective_N();
   v.cardioid_mode = h->outside_cardioid ? CARDIOID_NONE : CARDIOID_PER_SAMPLE;
   v.tol = h->view.tolerance();
   v.bailout2 = 1024.0 * 1024.0;
@@ -1145,16 +1189,17 @@ int noalloc_view(nm_handle* h, DeviceView& v, int& device, std::string& why, Ker
   v.coord_im = h->d_coord_im.p;
   v.eps_re = h->d_eps_re.p;
   v.eps_im = h->d_eps_im.p;
-  v.z = h->orbit_z();
-  v.zf = h->d_zf.p;
-  v.zlen = (int)h->od.z.size();
+  const nm_handle* t = h->tables();
+  v.z = t->orbit_z();
+  v.zf = t->d_zf.p;
+  v.zlen = (int)t->zlen();
   v.xlen = h->od.xlen;
-  v.xhi = h->d_xhi.p;
-  v.xlo = h->d_xlo.p;
-  v.sa_a = h->d_a.p;
-  v.sa_b = h->d_b.p;
-  v.sa_c = h->d_c.p;
-  v.sa_min = h->d_sa_min.p;
+  v.xhi = t->d_xhi.p;
+  v.xlo = t->d_xlo.p;
+  v.sa_a = t->d_a.p;
+  v.sa_b = t->d_b.p;
+  v.sa_c = t->d_c.p;
+  v.sa_min = t->d_sa_min.p;
   set_fe_tables(h, v);
   v.double_loop = h->od.double_loop ? 1 : 0;
   v.c_abs = coord_abs_bound(h);

@@ -100,8 +100,10 @@ struct nm_handle {
   // both copies
   DevBuf<nmg::Flt4> d_zf;
   const Dbl2* orbit_z() const {
-    return reinterpret_cast<const Dbl2*>(d_zf.p ? d_zf.p + od.z.size() : nullptr);
+    return reinterpret_cast<const Dbl2*>(d_zf.p ? d_zf.p + zlen() : nullptr);
   }
+  size_t zlen() const { return od_zlen ? od_zlen : od.z.size(); }
+  size_t od_zlen = 0;  // a sharing preview: its source's orbit length
   DevBuf<double> d_eps_re, d_eps_im, d_sa_min;
   // floatexp tables (views outside the FP64 range)
   std::vector<nmg::RFE> eps_re_fe, eps_im_fe;
@@ -119,6 +121,26 @@ struct nm_handle {
   // (orbit_stage.cuh), and a persisting L2 access-policy window on the orbit
   int z_stage = -1;  // -1: kAutoOrbitStage on floatexp views, else none
   bool l2_window = false;
+  // renders stop every sample at min(N, iter_cap) iterations (0: N); for
+  // previews that estimate where the work lies
+  int iter_cap = 0;
+  // A preview made by nm_preview reads its source's orbit and series tables
+  // (host and device) instead of holding copies; od then carries only the
+  // tables' sizes and flags.  The source must outlive the preview.
+  nm_handle* orbit_src = nullptr;
+  // Bumped whenever the handle's own orbit and series are replaced or dropped
+  // (nm_precompute, invalidate); a sharing preview records its source's stamp
+  // and refuses to render once the source has moved on.
+  unsigned long long tables_stamp = 0;
+  unsigned long long src_stamp = 0;
+  bool tables_stale() const {
+    return orbit_src && (!orbit_src->precomputed || orbit_src->tables_stamp != src_stamp);
+  }
+  nm_handle* tables() { return orbit_src ? orbit_src : this; }
+  const nm_handle* tables() const { return orbit_src ? orbit_src : this; }
+  int effective_N() const {
+    return iter_cap > 0 && iter_cap < view.iterations() ? iter_cap : view.iterations();
+  }
 
   // scratch: work counters, statistics, and the FE32 rework list
   DevBuf<unsigned long long> d_scratch;  // kScratchWords, layout below
@@ -176,9 +198,17 @@ struct nm_handle {
     precomputed = false;
     coords_valid = false;
     uploaded = false;
+    orbit_src = nullptr;
+    od_zlen = 0;
+    tables_stamp++;
     generation++;
   }
 };
+
+// The error of a render of a preview whose source changed its orbit and series
+// (or dropped them) after nm_preview.
+inline constexpr const char* kStalePreview =
+    "the preview's source view changed or was precomputed again since nm_preview: make a new preview";
 
 namespace nmg {
 

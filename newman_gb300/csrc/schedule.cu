@@ -470,7 +470,7 @@ int nm_tile_features(nm_handle* preview, int tile_w, int tile_h, float* out, int
   const unsigned int init[2] = {0x7f7fffffu, 0u};
   NM_CUDA(cudaMemcpyAsync(lohi.p, init, 8, cudaMemcpyHostToDevice, s));
   const long long n = (long long)nr * nc;
-  const int N = preview->view.iterations();
+  const int N = preview->effective_N();  // x = 1 at the preview's own cap
   nmg::note_launches(2);
   nmg::preview_range_kernel<<<256, 256, 0, s>>>(preview->grid.p, n, N, lohi.p);
   nmg::tile_features_kernel<<<(ntiles + 127) / 128, 128, 0, s>>>(

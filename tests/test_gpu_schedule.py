@@ -94,3 +94,14 @@ def test_preview_shares_the_orbit(nm):
     assert feats.shape == ((p.cols() // 4) * (p.rows() // 4), 18)
     assert np.allclose(feats[:, :16].sum(1), 1.0)
     assert (feats[:, 16] <= feats[:, 17] + 1e-7).all()
+    # an iteration cap renders as if N were the cap: min(full count, cap)
+    sub = full["iterations"][f - 1::f, ::f]
+    cap = int(np.median(sub))
+    p.set_option(nm.OPT_ITER_CAP, cap)
+    p.render()
+    assert np.array_equal(p.grid()["iterations"], np.minimum(sub, cap))
+    # the preview reads the view's orbit in place: a new precompute of the
+    # view makes it refuse to render rather than read tables that moved
+    m.precompute()
+    with pytest.raises(nm.NewmanError):
+        p.render()

@@ -330,7 +330,9 @@ class Mandelbrot:
         h = _lib.nm_copy(self._h)
         if not h:
             raise NewmanError(NM_ERR_CUDA, _lib.nm_last_error().decode())
-        return Mandelbrot(_handle=h)
+        c = Mandelbrot(_handle=h)
+        c._source = getattr(self, "_source", None)  # a preview's copy reads the same orbit
+        return c
 
     # ---- learned tile scheduling (no reference counterpart) -----------------
     def preview(self, factor):

@@ -928,6 +928,7 @@ nm_handle* nm_preview(const nm_handle* src, int factor) {
   }
   std::unique_ptr<nm_handle> h(new nm_handle(1, 1));
   h->view = src->view;
+  h->view.stand_in_for(src->view);  // the source's precision and arithmetic
   h->view.scale_down(factor);
   h->path = src->path;
   h->chunk = src->chunk;
@@ -938,7 +939,21 @@ nm_handle* nm_preview(const nm_handle* src, int factor) {
   if (src->precomputed && (src->reference_mode == nmg::REFERENCE_CENTER || src->od.double_loop)) {
     // the orbit at the view center and its series do not depend on the grid:
     // only the per-row / per-column tables are the preview's own
-    h->od = src->od;
+    if (src->od.double_loop) {
+      h->od = src->od;
+    } else {
+      // the orbit and series stay with their owner, read in place (host
+      // vectors and device tables): only their sizes and flags come along
+      const nm_handle* owner = src->tables();
+      h->orbit_src = const_cast<nm_handle*>(owner);
+      h->src_stamp = owner->tables_stamp;
+      h->od_zlen = owner->zlen();
+      h->od.xlen = src->od.xlen;
+      h->od.probe_index = src->od.probe_index;
+      h->od.sa_fp64_ok = src->od.sa_fp64_ok;
+      h->od.double_loop = false;
+      h->od.mp_limbs = src->od.mp_limbs;
+    }
     if (ensure_coords(h.get()) != NM_OK) return nullptr;
     if (h->od.double_loop) {
       std::vector<double> px(h->coord_re.size()), py(h->coord_im.size());
@@ -946,19 +961,6 @@ nm_handle* nm_preview(const nm_handle* src, int factor) {
       for (size_t r = 0; r < py.size(); r++) py[r] = h->coord_im[r].x;
       h->view.eps_tables_double_loop(px, py, h->eps_re, h->eps_im);
     } else {
-      // the orbit and series stay with their owner, read in place (host
-      // vectors and device tables): only their sizes and flags come along
-      const nm_handle* owner = src->tables();
-      h->orbit_src = const_cast<nm_handle*>(owner);
-      h->src_stamp = owner->tables_stamp;
-      nmg::OrbitData lite;
-      lite.xlen = src->od.xlen;
-      lite.probe_index = src->od.probe_index;
-      lite.sa_fp64_ok = src->od.sa_fp64_ok;
-      lite.double_loop = src->od.double_loop;
-      lite.mp_limbs = src->od.mp_limbs;
-      h->od = std::move(lite);
-      h->od_zlen = owner->zlen();
       h->view.eps_tables(h->od, h->eps_re, h->eps_im);
       if (!h->od.sa_fp64_ok) h->view.eps_tables_fe(h->eps_re_fe, h->eps_im_fe);
       build_front32_tables(h.get(), /*series=*/false);

@@ -271,6 +271,7 @@ int MPView::set_view(const char* cre, const char* cim, const char* sre, const ch
       mpf_set_str(t.p(), sim, 10) != 0)
     return 2;
   min_bits_ = min_bits > 0 ? (unsigned long)min_bits : 0;
+  no_hardware_ = false;
   mpf_set_prec(sre_.p(), 4096);
   mpf_set(sre_.p(), probe.p());
   set_precision();
@@ -287,7 +288,7 @@ void MPView::set_iterations(int N) { N_ = N; }
 
 bool MPView::use_hardware() const {
   const double minpreview = 1.5e-16;
-  return sre_.d() >= minpreview && sim_.d() >= minpreview;
+  return !no_hardware_ && sre_.d() >= minpreview && sim_.d() >= minpreview;
 }
 
 void MPView::scale_up(int sc) {
@@ -373,6 +374,7 @@ int MPView::load_legacy(const char* path) {
   std::fclose(fp);
   if (!ok) return 2;
   N_ = n;
+  no_hardware_ = false;  // a loaded view is nobody's preview
   Mpf f(64);
   mpf_set_d(f.p(), 800.0 / nc_);
   mpf_mul(sre_.p(), sre_.p(), f.p());

@@ -104,6 +104,13 @@ class MPView {
   void set_tolerance(double tol) { tol_ = tol; }
 
   bool use_hardware() const;  // mandelbrot.cpp:256-259
+  // A preview that stands for a finer view (nm_preview): it keeps the finer
+  // view's precision through scale_down, and renders by perturbation wherever
+  // the finer view does, whatever its own step.
+  void stand_in_for(const MPView& fine) {
+    min_bits_ = std::max(min_bits_, fine.bits_);
+    no_hardware_ = !fine.use_hardware();
+  }
   double step_max() const { return std::max(std::fabs(sre_.d()), std::fabs(sim_.d())); }
   void scale_up(int sc);      // mandelbrot.cpp:334-346 (geometry)
   void scale_down(int sc);    // mandelbrot.cpp:348-360 (geometry)
@@ -168,6 +175,7 @@ class MPView {
   int N_ = 256;
   double tol_ = 1e-10;
   unsigned long bits_ = 64, min_bits_ = 0;
+  bool no_hardware_ = false;
   Mpf cre_, cim_, sre_, sim_;
   Mpf x0re_, x0im_;  // X[0] of the last precompute
 };

@@ -100,8 +100,27 @@ def test_preview_shares_the_orbit(nm):
     p.set_option(nm.OPT_ITER_CAP, cap)
     p.render()
     assert np.array_equal(p.grid()["iterations"], np.minimum(sub, cap))
-    # the preview reads the view's orbit in place: a new precompute of the
-    # view makes it refuse to render rather than read tables that moved
+
+
+def test_preview_reads_the_orbit_in_place(nm):
+    """On a view past the double loop (a crop of C2 at its own sample
+    spacing, 64 bits) the preview reads the view's orbit and series in place:
+    it renders the view's samples, and once the view is precomputed again it
+    refuses to render rather than read tables that were replaced."""
+    v = dict(C2, nr=48, nc=80, N=20000)
+    m = setup_gpu(nm, v, path=nm.PATH_FE32)
+    m.set_option(nm.OPT_REFERENCE, nm.REFERENCE_CENTER)
     m.precompute()
-    with pytest.raises(nm.NewmanError):
-        p.render()
+    assert not m.useHardware()
+    m.render()
+    f = 4
+    p = m.preview(f)
+    p.render()
+    assert np.array_equal(p.grid(), m.grid()[f - 1::f, ::f])
+    q = p.copy()  # a copy of the preview shares the same orbit
+    q.render()
+    assert np.array_equal(q.grid(), p.grid())
+    m.precompute()
+    for h in (p, q):
+        with pytest.raises(nm.NewmanError):
+            h.render()

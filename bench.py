@@ -871,10 +871,14 @@ def learned_views(count=10, seed=5):
     return out
 
 
+PREVIEW_EXTRA = 512  # previews stop samples this many steps past the orbit's length
+
+
 def tile_log(nm, m, sc, tile_px=32, preview_px=8):
     """Per-tile features (from a preview with one sample per preview_px x
-    preview_px pixels) and the logged per-tile work of one whole render of m,
-    on tiles of tile_px x tile_px pixels."""
+    preview_px pixels, capped at the orbit length + PREVIEW_EXTRA) and the
+    logged per-tile work of one whole render of m, on tiles of tile_px x
+    tile_px pixels."""
     tile = tile_px * sc
     m.set_option(nm.OPT_TILE_W, tile)
     m.set_option(nm.OPT_TILE_H, tile)
@@ -886,6 +890,8 @@ def tile_log(nm, m, sc, tile_px=32, preview_px=8):
     p = m.preview(f)
     if not p.useHardware() and p.stat(nm.STAT_ORBIT_LENGTH) == 0:
         p.precompute()
+    if not p.useHardware():
+        p.set_option(nm.OPT_ITER_CAP, p.stat(nm.STAT_ORBIT_LENGTH) + PREVIEW_EXTRA)
     p.render()
     return p.tile_features(tile // f, tile // f), costs
 
@@ -937,7 +943,10 @@ def run_learned(args):
         X.append(feats)
         Y.append(centred_log(costs))
         train_info[name] = {"tiles": int(len(costs)), "cost_spread_log2": float(np.ptp(Y[-1]))}
+        if name == "C3":
+            c3_view, c3_costs = m, costs
         del m
+    train_views = None
     X, Y = np.concatenate(X), np.concatenate(Y)
     model = nm.CostModel(seed=2026)
     t0 = time.perf_counter()
@@ -945,13 +954,9 @@ def run_learned(args):
     train_s = time.perf_counter() - t0
     var = float(np.var(Y))
 
-    # the deep views
-    nr, nc, sc, N = 2160, 3840, 2, 2000000
-    rows, t_static, t_learned, t_oracle, t_over = [], 0.0, 0.0, 0.0, 0.0
-    identical = True
-    for vw in learned_views():
-        m = view(nr, nc, sc, vw["cre"], vw["cim"], vw["width"], N)
-        feats, costs = tile_log(nm, m, sc)  # tile size set, costs for the error report
+    def evaluate(m, sc, costs):
+        """Static, learned (capped preview + nm_order_tiles, timed) and
+        true-cost orders of one view; their images must agree."""
 
         def timed_render(order):
             m.set_tile_order(order)
@@ -963,30 +968,48 @@ def run_learned(args):
             return float(np.mean(ts)), m.grid()
 
         ms_static, g_static = timed_render(None)
-        # learned order: preview, features, prediction, sort -- all timed
+        torch.cuda.synchronize()
         t0 = time.perf_counter()
         p = m.preview(8 * sc)
+        if not p.useHardware():
+            p.set_option(nm.OPT_ITER_CAP, m.stat(nm.STAT_ORBIT_LENGTH) + PREVIEW_EXTRA)
         p.render()
-        f = p.tile_features(32 // 8, 32 // 8)
-        pred = model.predict(f)
-        order = np.argsort(-pred, kind="stable").astype(np.int32)
+        m.order_tiles(p, model)
+        torch.cuda.synchronize()
         over_ms = (time.perf_counter() - t0) * 1e3
+        order = m.tile_order()
+        pred = model.predict(p.tile_features(32 // 8, 32 // 8))  # for the error report (untimed)
         ms_learned, g_learned = timed_render(order)
         ms_oracle, g_oracle = timed_render(np.argsort(-costs, kind="stable").astype(np.int32))
         same = bool(np.array_equal(g_static, g_learned) and np.array_equal(g_static, g_oracle))
-        identical &= same
         y = centred_log(costs)
         err = pred - pred.mean() - y
-        rows.append({"width": vw["width"], "stop": vw["stop"], "orbit_length": m.stat(nm.STAT_ORBIT_LENGTH),
-                     "ms_static": ms_static, "ms_learned": ms_learned, "ms_overhead": over_ms,
-                     "ms_cost_order": ms_oracle, "identical": same,
-                     "spearman": spearman(pred, costs), "mae_log2": float(np.abs(err).mean()),
-                     "cost_spread_log2": float(np.ptp(y))})
-        t_static += ms_static
-        t_learned += ms_learned
-        t_over += over_ms
-        t_oracle += ms_oracle
-        del m, p
+        return {"orbit_length": m.stat(nm.STAT_ORBIT_LENGTH), "ms_static": ms_static,
+                "ms_learned": ms_learned, "ms_overhead": over_ms, "ms_cost_order": ms_oracle,
+                "speedup_with_overhead": ms_static / (ms_learned + over_ms),
+                "identical": same, "spearman": spearman(pred, costs),
+                "mae_log2": float(np.abs(err).mean()), "cost_spread_log2": float(np.ptp(y))}
+
+    # the 1e-300 view (C3), whose frame time its longest samples set
+    c3_row = evaluate(c3_view, 1, c3_costs)
+    del c3_view
+
+    # the deep views
+    nr, nc, sc, N = 2160, 3840, 2, 2000000
+    rows, t_static, t_learned, t_oracle, t_over = [], 0.0, 0.0, 0.0, 0.0
+    identical = c3_row["identical"]
+    for vw in learned_views():
+        m = view(nr, nc, sc, vw["cre"], vw["cim"], vw["width"], N)
+        feats, costs = tile_log(nm, m, sc)  # tile size set, costs for the error report
+        r = evaluate(m, sc, costs)
+        r.update({"width": vw["width"], "stop": vw["stop"]})
+        rows.append(r)
+        identical &= r["identical"]
+        t_static += r["ms_static"]
+        t_learned += r["ms_learned"]
+        t_over += r["ms_overhead"]
+        t_oracle += r["ms_cost_order"]
+        del m
     speedup = t_static / (t_learned + t_over)
     sp = [r["spearman"] for r in rows if r["spearman"] is not None]
     line = {
@@ -1002,6 +1025,7 @@ def run_learned(args):
         "train": {"tiles": int(len(Y)), "loss": loss, "target_variance": var, "seconds": train_s},
         "ms_static_total": t_static, "ms_learned_total": t_learned, "ms_overhead_total": t_over,
         "ms_cost_order_total": t_oracle, "speedup_without_overhead": t_static / t_learned,
+        "c3": c3_row,
         "speedup_cost_order": t_static / t_oracle, "bit_identical": identical,
         "prediction": {"spearman_mean": float(np.mean(sp)) if sp else None,
                        "mae_log2_mean": float(np.mean([r["mae_log2"] for r in rows]))},

@@ -262,6 +262,20 @@ int nm_cost_model_gradient(nm_costmodel* m, const float* features, const float* 
 int nm_cost_model_train(nm_costmodel* m, const float* features, const float* targets, int n,
                         int epochs, float lr, float* loss);
 
+/* The learned longest-first order, all on the GPU and asynchronous on h's
+   stream: the tile features of `preview` (a rendered nm_preview of h, or any
+   view whose grid divides h's by the same factor in both directions), the
+   model's forward pass and a sort by decreasing prediction (ties by tile id:
+   the order of a stable sort of -prediction) are enqueued after the
+   preview's render, and the result becomes h's tile order for its next
+   whole-grid renders, as nm_set_tile_order would make it.  h's tile size
+   must be a multiple of the preview factor; at most 16,384 tiles.  The
+   model's later calls wait for the order to be computed. */
+int nm_order_tiles(nm_handle* h, nm_handle* preview, nm_costmodel* m);
+/* The order in effect (nm_set_tile_order's or nm_order_tiles'), n entries;
+   NM_ERR_STATE under the static order. */
+int nm_get_tile_order(nm_handle* h, int* out, int n);
+
 /* Batches: many frames rendered together, e.g. every frame of a zoom video,
    each frame a handle with its own view, orbit, series skip and N (no
    reference counterpart; the reference renders one view at a time).  The

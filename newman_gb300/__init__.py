@@ -44,7 +44,7 @@ EXPORTS = (
     "nm_batch_create", "nm_batch_destroy", "nm_batch_add", "nm_batch_set_option",
     "nm_batch_render", "nm_batch_get_stat", "nm_batch_frames", "nm_batch_autotune",
     "nm_preview", "nm_tiles", "nm_set_tile_order", "nm_get_tile_costs", "nm_tile_features",
-    "nm_cost_model_create", "nm_cost_model_destroy", "nm_cost_model_params",
+    "nm_order_tiles", "nm_get_tile_order", "nm_cost_model_create", "nm_cost_model_destroy", "nm_cost_model_params",
     "nm_cost_model_set_params", "nm_cost_model_predict", "nm_cost_model_gradient",
     "nm_cost_model_train", "nm_palette_load", "nm_palette_save", "nm_palette_destroy",
     "nm_palette_cache", "nm_colorize", "nm_write_ppm", "nm_video_interpolate",
@@ -129,6 +129,8 @@ def load_library(path=LIB_PATH):
         "nm_set_tile_order": (i32, [vp, vp, i32]),
         "nm_get_tile_costs": (i32, [vp, vp, i32]),
         "nm_tile_features": (i32, [vp, i32, i32, vp, i32]),
+        "nm_order_tiles": (i32, [vp, vp, vp]),
+        "nm_get_tile_order": (i32, [vp, vp, i32]),
         "nm_cost_model_create": (vp, [ctypes.c_ulonglong]),
         "nm_cost_model_destroy": (None, [vp]),
         "nm_cost_model_params": (i32, [vp, vp, i32]),
@@ -360,6 +362,21 @@ class Mandelbrot:
             return
         o = np.ascontiguousarray(order, dtype=np.int32)
         _check(_lib.nm_set_tile_order(self._h, o.ctypes.data, o.size))
+
+    def order_tiles(self, preview, model):
+        """The cost model's longest-first order from a rendered preview, computed
+        on the GPU after the preview's render (nm_order_tiles); no host round trip."""
+        _check(_lib.nm_order_tiles(self._h, preview._h, model._m))
+
+    def tile_order(self):
+        """The tile order in effect, or None under the static order."""
+        tx, ty = self.tiles()
+        out = np.empty(tx * ty, np.int32)
+        rc = _lib.nm_get_tile_order(self._h, out.ctypes.data, out.size)
+        if rc == NM_ERR_STATE:
+            return None
+        _check(rc)
+        return out
 
     def tile_costs(self):
         """Per-tile work of the last whole-grid render (NM_OPT_LOG_TILE_COSTS),

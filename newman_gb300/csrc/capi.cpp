@@ -77,7 +77,9 @@ namespace {
 
 // The CUDA side of a handle is created on first use, so that the host-only
 // calls (view edits, the arbitrary-precision precompute) work without a GPU.
-int ensure_device(nm_handle* h) {
+}  // namespace
+
+int nmg::ensure_device(nm_handle* h) {
   if (h->stream) return NM_OK;
   NM_CUDA(cudaGetDevice(&h->device));
   NM_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
@@ -89,6 +91,10 @@ int ensure_device(nm_handle* h) {
   for (cudaEvent_t& e : h->ev) NM_CUDA(cudaEventCreate(&e));
   return NM_OK;
 }
+
+namespace {
+
+using nmg::ensure_device;
 
 int ensure_grid(nm_handle* h) {
   if (int rc = ensure_device(h)) return rc;
@@ -370,10 +376,12 @@ int nmg::prepare_view(nm_handle* h, int r0, int r1, nmg::DeviceView& v, nmg::Ker
   v.grid = h->grid.p;
   v.smooth64 = h->keep_smooth64 ? h->smooth64.p : nullptr;
   const bool whole = r0 == 0 && r1 == nr;
-  if (whole && !h->tile_order.empty() && h->tile_order_w == h->tile_w &&
-      h->tile_order_h == h->tile_h &&
-      (long long)h->tile_order.size() == (long long)v.tiles_x * v.tiles_y) {
-    if (!h->tile_order_uploaded) {
+  const long long ntiles = (long long)v.tiles_x * v.tiles_y;
+  const bool host_order = !h->tile_order.empty() && (long long)h->tile_order.size() == ntiles;
+  const bool device_order = h->tile_order_on_device && h->tile_order_n == ntiles;
+  if (whole && (host_order || device_order) && h->tile_order_w == h->tile_w &&
+      h->tile_order_h == h->tile_h) {
+    if (host_order && !h->tile_order_uploaded) {
       if (int rc = upload(h->d_tile_order, h->tile_order, h->stream)) return rc;
       NM_CUDA(cudaStreamSynchronize(h->stream));
       h->tile_order_uploaded = true;
@@ -441,6 +449,15 @@ nm_handle* nm_copy(const nm_handle* src) {
   h->z_stage = src->z_stage;
   h->l2_window = src->l2_window;
   h->tile_order = src->tile_order;
+  if (src->tile_order_on_device && src->d_tile_order.p) {  // the copy holds it on the host
+    h->tile_order.resize((size_t)src->tile_order_n);
+    if (cudaStreamSynchronize(src->stream) != cudaSuccess ||
+        cudaMemcpy(h->tile_order.data(), src->d_tile_order.p, h->tile_order.size() * 4,
+                   cudaMemcpyDeviceToHost) != cudaSuccess) {
+      fail(NM_ERR_CUDA, "copy of a device tile order");
+      return nullptr;
+    }
+  }
   h->tile_order_w = src->tile_order_w;
   h->tile_order_h = src->tile_order_h;
   h->log_costs = src->log_costs;
@@ -882,6 +899,7 @@ int nm_tiles(nm_handle* h, int* tiles_x, int* tiles_y) {
 int nm_set_tile_order(nm_handle* h, const int* order, int n) {
   if (int rc = check_handle(h)) return rc;
   if (!order || n == 0) {
+    h->tile_order_on_device = false;
     h->tile_order.clear();
     h->generation++;
     return NM_OK;
@@ -897,10 +915,28 @@ int nm_set_tile_order(nm_handle* h, const int* order, int n) {
     seen[(size_t)order[k]] = 1;
   }
   h->generation++;
+  h->tile_order_on_device = false;
   h->tile_order.assign(order, order + n);
   h->tile_order_w = h->tile_w;
   h->tile_order_h = h->tile_h;
   h->tile_order_uploaded = false;
+  return NM_OK;
+}
+
+int nm_get_tile_order(nm_handle* h, int* out, int n) {
+  if (int rc = check_handle(h)) return rc;
+  if (!out) return fail(NM_ERR_ARG, "null output");
+  if (h->tile_order_on_device) {
+    if ((long long)n != h->tile_order_n)
+      return fail(NM_ERR_ARG, "%d entries for an order of %lld tiles", n, h->tile_order_n);
+    NM_CUDA(cudaStreamSynchronize(h->stream));
+    NM_CUDA(cudaMemcpy(out, h->d_tile_order.p, (size_t)n * 4, cudaMemcpyDeviceToHost));
+    return NM_OK;
+  }
+  if (h->tile_order.empty()) return fail(NM_ERR_STATE, "no tile order set (static order)");
+  if ((size_t)n != h->tile_order.size())
+    return fail(NM_ERR_ARG, "%d entries for an order of %zu tiles", n, h->tile_order.size());
+  std::memcpy(out, h->tile_order.data(), (size_t)n * 4);
   return NM_OK;
 }
 

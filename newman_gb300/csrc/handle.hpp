@@ -169,6 +169,10 @@ struct nm_handle {
   int tile_order_w = 0, tile_order_h = 0;
   bool tile_order_uploaded = false;
   DevBuf<int32_t> d_tile_order;
+  // an order computed on the GPU (nm_order_tiles): d_tile_order holds
+  // tile_order_n entries and the host vector is empty
+  bool tile_order_on_device = false;
+  long long tile_order_n = 0;
   bool log_costs = false;
   DevBuf<unsigned long long> d_tile_cost;
   long long cost_tiles = 0;
@@ -215,5 +219,7 @@ namespace nmg {
 // Everything a render of rows [r0, r1) of h needs on the GPU (grid, tables),
 // and the device view and kernel that render them (capi.cpp).
 int prepare_view(nm_handle* h, int r0, int r1, DeviceView& v, KernelKind& kind);
+// The handle's stream, scratch and events, created on first use.
+int ensure_device(nm_handle* h);
 
 }  // namespace nmg

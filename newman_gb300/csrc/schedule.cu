@@ -286,6 +286,44 @@ __global__ void adam_kernel(float* params, float* grad, float* m, float* v, __ha
   if (h >= 0) wh[h] = __float2half_rn(w);
 }
 
+// ---- longest-first order on the GPU ------------------------------------------
+//
+// One block sorts the tiles by key = (order-preserving bits of -prediction)
+// << 32 | tile id, ascending, in shared memory (bitonic network over the
+// next power of two, padding keys all ones): tiles by decreasing prediction,
+// ties by id -- the permutation a stable sort of -prediction gives.
+constexpr int kMaxOrderTiles = 16384;
+constexpr int kSortThreads = 1024;
+
+__device__ __forceinline__ uint32_t order_bits(float x) {
+  const uint32_t b = __float_as_uint(x == 0.0f ? 0.0f : x);  // -0 ties with +0
+  return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+
+__global__ void __launch_bounds__(kSortThreads) order_sort_kernel(const float* __restrict__ pred,
+                                                                  int n, int p2,
+                                                                  int32_t* __restrict__ order) {
+  extern __shared__ unsigned long long keys[];
+  for (int k = threadIdx.x; k < p2; k += blockDim.x)
+    keys[k] = k < n ? ((unsigned long long)order_bits(-pred[k]) << 32) | (unsigned)k : ~0ull;
+  __syncthreads();
+  for (int size = 2; size <= p2; size <<= 1) {
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int t = threadIdx.x; t < (p2 >> 1); t += blockDim.x) {
+        const int lo = 2 * t - (t & (stride - 1));  // t with a 0 inserted at bit log2(stride)
+        const int hi = lo + stride;
+        const unsigned long long a = keys[lo], b = keys[hi];
+        if ((a > b) == ((lo & size) == 0)) {
+          keys[lo] = b;
+          keys[hi] = a;
+        }
+      }
+      __syncthreads();
+    }
+  }
+  for (int k = threadIdx.x; k < n; k += blockDim.x) order[k] = (int32_t)(keys[k] & 0xffffffffull);
+}
+
 int mlp_blocks(int n, int device) {
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
@@ -302,6 +340,7 @@ struct nm_costmodel {
   nmg::DevBuf<float> params, grad, m, v, scratch;
   nmg::DevBuf<__half> wh;
   nmg::DevBuf<float> x, t, y;
+  nmg::DevBuf<unsigned int> lohi;  // the preview's log-count range (nm_order_tiles)
   long long step = 0;
   ~nm_costmodel() {
     if (stream) cudaStreamDestroy(stream);
@@ -330,12 +369,13 @@ int stage(nm_costmodel* m, const float* x, const float* t, int n) {
 }
 
 template <bool kTrain>
-int launch_mlp(nm_costmodel* m, int n, float* out) {
+int launch_mlp(nm_costmodel* m, int n, float* out, cudaStream_t stream = nullptr) {
   const size_t smem = sizeof(nmg::MlpShared);
   NM_CUDA(cudaFuncSetAttribute(nmg::mlp_kernel<kTrain>,
                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   nmg::note_launches(1);
-  nmg::mlp_kernel<kTrain><<<nmg::mlp_blocks(n, m->device), nmg::kH, smem, m->stream>>>(
+  nmg::mlp_kernel<kTrain><<<nmg::mlp_blocks(n, m->device), nmg::kH, smem,
+                            stream ? stream : m->stream>>>(
       m->wh.p, m->params.p, m->x.p, kTrain ? m->t.p : nullptr, n, out, m->grad.p,
       m->scratch.p);
   NM_CUDA(cudaGetLastError());
@@ -478,6 +518,68 @@ int nm_tile_features(nm_handle* preview, int tile_w, int tile_h, float* out, int
   NM_CUDA(cudaGetLastError());
   NM_CUDA(cudaMemcpyAsync(out, d_out.p, (size_t)ntiles * nmg::kIn * 4, cudaMemcpyDeviceToHost, s));
   NM_CUDA(cudaStreamSynchronize(s));
+  return NM_OK;
+}
+
+int nm_order_tiles(nm_handle* h, nm_handle* preview, nm_costmodel* m) {
+  if (!h || !preview || !m) return fail(NM_ERR_ARG, "order tiles: null argument");
+  if (!preview->stream || !preview->grid.p) return fail(NM_ERR_STATE, "preview not rendered");
+  const int nr = h->view.rows(), nc = h->view.cols();
+  const int pr = preview->grid_nr, pc = preview->grid_nc;
+  if (pr < 1 || pc < 1 || nr % pr || nc % pc || nr / pr != nc / pc)
+    return fail(NM_ERR_ARG, "a %d x %d preview of a %d x %d view", pr, pc, nr, nc);
+  const int f = nr / pr;
+  if (h->tile_w % f || h->tile_h % f)
+    return fail(NM_ERR_ARG, "tile %d x %d is not a multiple of the preview factor %d", h->tile_w,
+                h->tile_h, f);
+  const int tw = h->tile_w / f, th = h->tile_h / f;
+  const int tx = (nc + h->tile_w - 1) / h->tile_w, ty = (nr + h->tile_h - 1) / h->tile_h;
+  const long long ntiles = (long long)tx * ty;  // == the preview's tiles of tw x th
+  if (ntiles > nmg::kMaxOrderTiles)
+    return fail(NM_ERR_UNSUPPORTED, "%lld tiles (at most %d)", ntiles, nmg::kMaxOrderTiles);
+  if (int rc = nmg::ensure_device(h)) return rc;
+  cudaStream_t s = h->stream;
+  // after the preview's render, and after the model's own pending work
+  cudaEvent_t ev = nullptr;
+  NM_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  NM_CUDA(cudaEventRecord(ev, preview->render_stream ? preview->render_stream : preview->stream));
+  NM_CUDA(cudaStreamWaitEvent(s, ev, 0));
+  NM_CUDA(cudaEventRecord(ev, m->stream));
+  NM_CUDA(cudaStreamWaitEvent(s, ev, 0));
+  NM_CUDA(m->lohi.reserve(2));
+  NM_CUDA(m->x.reserve((size_t)ntiles * nmg::kIn));
+  NM_CUDA(m->y.reserve((size_t)ntiles));
+  NM_CUDA(h->d_tile_order.reserve((size_t)ntiles));
+  const unsigned int init[2] = {0x7f7fffffu, 0u};
+  NM_CUDA(cudaMemcpyAsync(m->lohi.p, init, 8, cudaMemcpyHostToDevice, s));
+  const long long n = (long long)pr * pc;
+  const int N = preview->effective_N();
+  nmg::note_launches(2);
+  nmg::preview_range_kernel<<<256, 256, 0, s>>>(preview->grid.p, n, N, m->lohi.p);
+  nmg::tile_features_kernel<<<(int)((ntiles + 127) / 128), 128, 0, s>>>(
+      preview->grid.p, pr, pc, N, tw, th, tx, (int)ntiles, m->lohi.p, m->x.p);
+  NM_CUDA(cudaGetLastError());
+  if (int rc = launch_mlp<false>(m, (int)ntiles, m->y.p, s)) return rc;
+  int p2 = 2;
+  while (p2 < ntiles) p2 <<= 1;
+  const size_t smem = (size_t)p2 * sizeof(unsigned long long);
+  NM_CUDA(cudaFuncSetAttribute(nmg::order_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem));
+  nmg::note_launches(1);
+  nmg::order_sort_kernel<<<1, nmg::kSortThreads, smem, s>>>(m->y.p, (int)ntiles, p2,
+                                                              h->d_tile_order.p);
+  NM_CUDA(cudaGetLastError());
+  // the model's next calls (which reuse x and y) wait for the sort
+  NM_CUDA(cudaEventRecord(ev, s));
+  NM_CUDA(cudaStreamWaitEvent(m->stream, ev, 0));
+  NM_CUDA(cudaEventDestroy(ev));
+  h->tile_order.clear();
+  h->tile_order_on_device = true;
+  h->tile_order_n = ntiles;
+  h->tile_order_w = h->tile_w;
+  h->tile_order_h = h->tile_h;
+  h->tile_order_uploaded = true;
+  h->generation++;
   return NM_OK;
 }
 

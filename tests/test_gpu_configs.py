@@ -11,6 +11,9 @@
 * One learned-scheduling view (3840x2160, 2x2 samples, N 2,000,000): the
   render in the cost model's longest-first tile order against the static
   order, bit-identical.
+* The 1e-300 view in the order the cost model predicts from a capped preview
+  (computed on the GPU): bit-identical to the static order and a shorter
+  render; the times with and without the preview are recorded.
 
 Measured fractions are written as JSON when NM_TEST_RECORD names a file
 prefix.
@@ -158,3 +161,106 @@ def test_c5_learned_order_bit_identical(nm):
     m.render()
     learned = m.grid()
     assert np.array_equal(static, learned)
+
+
+def _tile_log(nm, m, tile, f, extra=512):
+    """Tile costs of one whole render of m (tiles of tile x tile samples) and
+    the features of a preview one sample per f x f, its iterations capped at
+    the orbit length + extra (where the view has an orbit)."""
+    m.set_option(nm.OPT_TILE_W, tile)
+    m.set_option(nm.OPT_TILE_H, tile)
+    m.set_option(nm.OPT_LOG_TILE_COSTS, 1)
+    m.render()
+    costs = m.tile_costs().astype(np.float64).ravel()
+    m.set_option(nm.OPT_LOG_TILE_COSTS, 0)
+    p = m.preview(f)
+    if not p.useHardware():
+        p.set_option(nm.OPT_ITER_CAP, m.stat(nm.STAT_ORBIT_LENGTH) + extra)
+    p.render()
+    return p.tile_features(tile // f, tile // f), costs
+
+
+def test_c3_learned_order_gain(nm):
+    """What the trained network gains on the 1e-300 view, whose frame time is
+    set by its longest samples: the model is trained on the tile costs its
+    own renders logged on C1, C2 and C3 (32x32-pixel tiles), then orders C3's
+    tiles from a capped preview on the GPU (nm_order_tiles).  The render in
+    that order is bit-identical to the static order's and shorter; the
+    recorded times give the gain with and without the preview (measured:
+    render 31.9 -> 29.6 ms, order by the true costs 28.3 ms, preview and
+    ordering ~3.3 ms)."""
+    import time
+    import torch
+    from decimal import Decimal, getcontext
+    getcontext().prec = 700
+    nr, nc, N, bits = 2160, 3840, 1000000, 1100
+    cre, cim, step = deep_view(72, nc)
+
+    def view(nr, nc, sc, cre, cim, step, N, bits=0):
+        m = nm.Mandelbrot(nr, nc)
+        m.set_view(cre, cim, step, step, N, 1e-10, bits)
+        if sc > 1:
+            m.scaleUp(sc)
+        if not m.useHardware():
+            m.set_path(nm.PATH_FE32)
+            m.set_option(nm.OPT_REFERENCE, nm.REFERENCE_CENTER)
+            m.precompute()
+        return m
+
+    c1 = view(480, 640, 1, "-0.75", "0", "0.0046875", 1024)
+    c2 = view(1080, 1920, 4, "-0.743643887037151", "0.131825904205330",
+              str(Decimal("1e-12") / 1920), 50000)
+    c3 = view(nr, nc, 1, cre, cim, step, N, bits)
+    logs = [_tile_log(nm, c1, 32, 8), _tile_log(nm, c2, 128, 32), _tile_log(nm, c3, 32, 8)]
+    X = np.concatenate([x for x, _ in logs])
+    Y = np.concatenate([np.log2(1.0 + c) - np.log2(1.0 + c).mean() for _, c in logs])
+    model = nm.CostModel(seed=2026)
+    model.train(X, Y.astype(np.float32), epochs=300, lr=2e-3)
+    costs = logs[2][1]
+
+    def kernel_ms(n=5):
+        c3.render()
+        ts = []
+        for _ in range(n):
+            c3.render()
+            ts.append(c3.stat(nm.STAT_KERNEL_NS) * 1e-6)
+        return float(np.median(ts))
+
+    def wall_ms(fn, n=5):
+        ts = []
+        for _ in range(n):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            ts.append((time.perf_counter() - t0) * 1e3)
+        return float(np.median(ts))
+
+    c3.set_tile_order(None)
+    static_ms = kernel_ms()
+    static = c3.grid().copy()
+    static_wall = wall_ms(c3.render)
+
+    def learned():
+        p = c3.preview(8)
+        p.set_option(nm.OPT_ITER_CAP, c3.stat(nm.STAT_ORBIT_LENGTH) + 512)
+        p.render()
+        c3.order_tiles(p, model)
+        c3.render()
+
+    learned_wall = wall_ms(learned)
+    order = c3.tile_order()
+    learned_ms = kernel_ms()
+    assert np.array_equal(c3.grid(), static)
+    c3.set_tile_order(np.argsort(-costs, kind="stable").astype(np.int32))
+    cost_order_ms = kernel_ms()
+    assert np.array_equal(c3.grid(), static)
+    rank = lambda a: np.argsort(np.argsort(a))
+    position = np.empty_like(order)
+    position[order] = np.arange(len(order))
+    _record("c3_learned_order", {
+        "render_ms_static": static_ms, "render_ms_learned": learned_ms,
+        "render_ms_true_cost_order": cost_order_ms, "wall_ms_static": static_wall,
+        "wall_ms_learned_with_preview": learned_wall,
+        "spearman_order_vs_costs": float(np.corrcoef(rank(-position), rank(costs))[0, 1])})
+    assert learned_ms < static_ms

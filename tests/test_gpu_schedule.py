@@ -124,3 +124,35 @@ def test_preview_reads_the_orbit_in_place(nm):
     for h in (p, q):
         with pytest.raises(nm.NewmanError):
             h.render()
+
+
+def test_order_tiles_on_the_gpu(nm):
+    """nm_order_tiles: features, forward pass and sort on the GPU give the
+    permutation of a stable host sort of -prediction, and the render under it
+    is the static order's image bit for bit."""
+    v = dict(C2, nr=64, nc=96, N=20000)
+    m = setup_gpu(nm, v, path=nm.PATH_FE32)
+    m.set_option(nm.OPT_REFERENCE, nm.REFERENCE_CENTER)
+    m.precompute()
+    m.set_option(nm.OPT_TILE_W, 16)
+    m.set_option(nm.OPT_TILE_H, 16)
+    m.render()
+    ref = m.grid()
+    assert m.tile_order() is None
+    f = 4
+    p = m.preview(f)
+    p.render()
+    model = nm.CostModel(seed=5)
+    X = p.tile_features(16 // f, 16 // f)
+    model.train(X, np.linspace(-1, 1, len(X)).astype(np.float32), epochs=50, lr=3e-3)
+    pred = model.predict(X)
+    m.order_tiles(p, model)
+    order = m.tile_order()
+    assert np.array_equal(order, np.argsort(-pred, kind="stable"))
+    assert np.array_equal(model.predict(X), pred)  # the model's inputs were not disturbed
+    m.render()
+    assert np.array_equal(m.grid(), ref)
+    c = m.copy()  # a copy carries the order (read back to the host)
+    assert np.array_equal(c.tile_order(), order)
+    m.set_tile_order(None)
+    assert m.tile_order() is None

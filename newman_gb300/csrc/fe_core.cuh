@@ -45,7 +45,32 @@ constexpr float kFeUZ = 0x1p-45f;     // Z's representation and the rounding of 
 // (both inputs' low words are within 2^-24 of their high words, and t.h is
 // their sum rounded once more), so
 //   u |t.h|_1 |delta| + u_z (2|Z| + |delta|) |delta| <= kFeUT (2|Z| + |delta|) |delta|.
+// (u in units of 2^-48 and of A = the sum of a component's two |t.h||delta.h|
+// products, C = |eps.h|: the eight roundings into the low word 30 A + 8 C, the
+// final fast two-sum -- not exact when the high part cancels below the low
+// word -- at most 2^-24 of the low word, 5 A + 2 C, the dropped t.l delta.l
+// products A: 36 A + 10 C.)
 constexpr float kFeUT = 0x1.61p-43f;
+// The same two terms when t enters the multiply-add unnormalised
+// (ff_add_twice_raw, 6 FP32 additions a step fewer): t.h = RN(2 Z.h + delta.h),
+// |t.l| <= 2^-23 T with T = 2|Z.h| + |delta.h| per component, so a cross term
+// t.l delta.h reaches 2^-23 T |delta.h| instead of 2^-24 |t.h||delta.h|.  With
+// B = the sum of a component's T |delta.h| (A <= B (1 + 2^-24)): roundings
+// 26 A + 8 B + 8 C, final fast two-sum 4 A + 2 B + 2 C, dropped products 2 B,
+// 42.5 B + 10 C with the (1 + 2^-24) factors.  The components' B add up to
+// P' = (2|Z.h|_1 + |delta.h|_1) |delta.h|_1, so the step rounds by at most
+// 1.33 * 2^-43 P' + u |eps|_1, and with u_z kFeUTRaw = 1.578125 * 2^-43.
+// Both assume the delta a step reads is normalised, which the final fast
+// two-sum gives unless the new delta cancels below its own low word; what the
+// next step then rounds or drops beyond the derivation is below 2^-60 of
+// (|Z| + |delta|) times the carried bound's own local term, inside the 2^-20
+// margin on |Y| in the amplification.
+constexpr float kFeUTRaw = 0x1.94p-43f;
+// t = 2Z + delta for the step's multiply-add, renormalised or not.
+template <bool kRawT>
+__device__ __forceinline__ FF fe_twice_plus(float ah, float al, FF b) {
+  return kRawT ? ff_add_twice_raw(ah, al, b) : ff_add_twice(ah, al, b);
+}
 // A bound below which the bailout test of a state with |Y|^2 <= 2^20 (1 - 2^-10)
 // and Z not the orbit's escaped last point is decided without evaluating it:
 // |Z.h|_1 < 1449, |delta.h|_1 < 2900, so the band of the full test,
@@ -397,7 +422,7 @@ __device__ __forceinline__ void fe_renormalise(FeState& st) {
 // Steps while delta is scaled: Y = Z to working precision, so the events are
 // the reference's own escape, the end of the orbit, and Z passing so close to
 // 0 that |Y| < |delta| could hold (left to the FP64 kernel: uncertified).
-template <bool kStaged = false>
+template <bool kStaged = false, bool kRawT = false>
 __device__ __forceinline__ bool fe_scaled_steps(const DeviceView& v, FeState& st, int steps,
                                              FeResult& res, unsigned long long& executed,
                                              unsigned long long& rebases) {
@@ -409,8 +434,8 @@ __device__ __forceinline__ bool fe_scaled_steps(const DeviceView& v, FeState& st
   for (; st.i < stop; st.i++) {
     const FF sd_r = st.E < -140 ? FF{0.f, 0.f} : ff_scale(st.dr, st.E);
     const FF sd_i = st.E < -140 ? FF{0.f, 0.f} : ff_scale(st.di, st.E);
-    const FF tr = ff_add_twice(z.hx, z.lx, sd_r);
-    const FF ti = ff_add_twice(z.hy, z.ly, sd_i);
+    const FF tr = fe_twice_plus<kRawT>(z.hx, z.lx, sd_r);
+    const FF ti = fe_twice_plus<kRawT>(z.hy, z.ly, sd_i);
     const float zl1 = up_add(fabsf(z.hx), fabsf(z.hy)), dl1 = up_add(fabsf(st.dr.h), fabsf(st.di.h));
     FF nr, ni;
     ff_cmul_add(tr, ti, st.dr, st.di, st.er, st.ei, nr, ni);
@@ -420,7 +445,7 @@ __device__ __forceinline__ bool fe_scaled_steps(const DeviceView& v, FeState& st
       const float dmag = fmaxf(ldexpf(dl1, st.E), 0x1p-126f);
       const float amp = up_add(up_mul(2.0f, up_add(zl1, dmag)),
                                fmaxf(ldexpf(st.err, st.E), 0x1p-126f));
-      const float loc = up_fma(kFeUT, up_mul(up_fma(2.0f, zl1, dmag), dl1),
+      const float loc = up_fma(kRawT ? kFeUTRaw : kFeUT, up_mul(up_fma(2.0f, zl1, dmag), dl1),
                                up_mul(kFeU, up_add(fabsf(st.er.h), fabsf(st.ei.h))));
       st.err = up_fma(amp, st.err, loc);
     }
@@ -488,7 +513,7 @@ __device__ __forceinline__ bool fe_scaled_steps(const DeviceView& v, FeState& st
 // the iteration stops at once and res is not meaningful -- the sample goes to
 // the FP64 kernel.
 // The unscaled steps; kDl: a double-loop view (second bound e64, trapping).
-template <bool kDl, bool kStaged = false>
+template <bool kDl, bool kStaged = false, bool kRawT = false>
 __device__ __forceinline__ bool fe_unscaled_steps(const DeviceView& v, FeState& st, int steps,
                                                   FeResult& res, unsigned long long& executed,
                                                   unsigned long long& rebases, FeTrap* trap) {
@@ -514,11 +539,11 @@ __device__ __forceinline__ bool fe_unscaled_steps(const DeviceView& v, FeState& 
   float ym = approx_norm(z.hx + dr.h, z.hy + di.h);
   bool done = false;
   for (; i < stop; i++) {
-    const FF tr = ff_add_twice(z.hx, z.lx, dr);
-    const FF ti = ff_add_twice(z.hy, z.ly, di);
+    const FF tr = fe_twice_plus<kRawT>(z.hx, z.lx, dr);
+    const FF ti = fe_twice_plus<kRawT>(z.hy, z.ly, di);
     const float zl1 = up_add(fabsf(z.hx), fabsf(z.hy)), dl1 = up_add(fabsf(dr.h), fabsf(di.h));
     const float ym_up = up_fma(0x1p-20f, up_add(zl1, dl1), ym);
-    const float loc = up_fma(kFeUT, up_mul(up_fma(2.0f, zl1, dl1), dl1), ueps);
+    const float loc = up_fma(kRawT ? kFeUTRaw : kFeUT, up_mul(up_fma(2.0f, zl1, dl1), dl1), ueps);
     const float err_old = err;
     err = up_fma(up_fma(2.0f, ym_up, err), err, loc);  // 2|Y| e + e^2 + local rounding
     FF nr, ni;
@@ -656,7 +681,7 @@ __device__ __forceinline__ bool fe_unscaled_steps(const DeviceView& v, FeState& 
   return false;
 }
 
-template <bool kStaged = false>
+template <bool kStaged = false, bool kRawT = false>
 __device__ __forceinline__ bool fe_advance(const DeviceView& v, FeState& st, int steps,
                                            FeResult& res, unsigned long long& executed,
                                            unsigned long long& rebases, FeTrap* trap = nullptr) {
@@ -665,11 +690,11 @@ __device__ __forceinline__ bool fe_advance(const DeviceView& v, FeState& st, int
       st.certified = 0;
       return true;
     }
-    return fe_scaled_steps<kStaged>(v, st, steps, res, executed, rebases);
+    return fe_scaled_steps<kStaged, kRawT>(v, st, steps, res, executed, rebases);
   }
   if (v.double_loop)
-    return fe_unscaled_steps<true, kStaged>(v, st, steps, res, executed, rebases, trap);
-  return fe_unscaled_steps<false, kStaged>(v, st, steps, res, executed, rebases, nullptr);
+    return fe_unscaled_steps<true, kStaged, kRawT>(v, st, steps, res, executed, rebases, trap);
+  return fe_unscaled_steps<false, kStaged, kRawT>(v, st, steps, res, executed, rebases, nullptr);
 }
 
 }  // namespace nmg

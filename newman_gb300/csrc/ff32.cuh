@@ -48,6 +48,17 @@ NM_HD FF ff_add_twice(float ah, float al, FF b) {
   const float e = fadd_(ffma_(2.0f, ah, -fsub_(s, bb)), fsub_(b.h, bb));
   return ff_fast_two_sum(s, fadd_(e, ffma_(2.0f, al, b.l)));
 }
+// ff_add_twice without the final renormalisation: h = RN(2 ah + b.h), l = its
+// exact error plus 2 al + b.l (rounded twice).  h + l is ff_add_twice's value
+// (the renormalisation is exact), but l is not bounded by half an ulp of h:
+// |l| <= 2^-23 (2|ah| + |b.h|), and more than |h| where 2 ah + b.h cancels.
+// For operands that only enter products (the FE32 step's t = 2Z + delta).
+NM_HD FF ff_add_twice_raw(float ah, float al, FF b) {
+  const float s = ffma_(2.0f, ah, b.h);
+  const float bb = ffma_(-2.0f, ah, s);
+  const float e = fadd_(ffma_(2.0f, ah, -fsub_(s, bb)), fsub_(b.h, bb));
+  return FF{s, fadd_(e, ffma_(2.0f, al, b.l))};
+}
 NM_HD FF ff_from_double(double x) {
   const float h = (float)x;
   return {h, (float)(x - (double)h)};

@@ -26,6 +26,8 @@
 //   persistent kernel (the FP64 front inside the refill loop).  Its scratch is only the
 //   work counters and the rework list, which lets the allocation-free entry
 //   point (noalloc.cu) run it from a fixed static array.
+#include <type_traits>
+
 #include "engine.hpp"
 #include "fe_core.cuh"
 #include "jobs_fp64.cuh"
@@ -36,6 +38,7 @@ namespace nmg {
 
 namespace {
 
+template <bool kRawT>
 struct FeJob {
   using State = FeState;
   static constexpr bool kCertifies = true;
@@ -50,7 +53,7 @@ struct FeJob {
                                                unsigned long long& executed,
                                                unsigned long long& rebases) {
     FeResult res;
-    if (!fe_advance(v, st, n, res, executed, rebases)) return false;
+    if (!fe_advance<false, kRawT>(v, st, n, res, executed, rebases)) return false;
     const float s = fe_smoothing(v, res);
     sm = s;
     out = {res.it, s};
@@ -61,9 +64,10 @@ struct FeJob {
   }
 };
 
+template <bool kRawT>
 __global__ void __launch_bounds__(kPersistentThreads) fe32_kernel(DeviceView v, RenderCtl ctl,
                                                                     int chunk) {
-  persistent_loop<FeJob>(v, ctl, chunk);
+  persistent_loop<FeJob<kRawT>>(v, ctl, chunk);
 }
 
 // ---- pass pipeline ------------------------------------------------------------
@@ -123,7 +127,7 @@ static_assert(sizeof(FeResult) == kFeResultBytes, "FE32 result record");
 
 // Persistent and warp-refilled like persistent_loop, over the work list: the
 // start state comes from the front pass, the result goes to the grid.
-template <bool kStaged = false>
+template <bool kStaged = false, bool kRawT = false>
 __device__ __forceinline__ void fe_iter_warp(const DeviceView& v, const FePassBuffers& b,
                                              const RenderCtl& ctl, int chunk) {
   const unsigned kFull = 0xffffffffu;
@@ -161,7 +165,7 @@ __device__ __forceinline__ void fe_iter_warp(const DeviceView& v, const FePassBu
     if (!__any_sync(kFull, active)) break;
     if (active) {
       FeResult res;
-      if (fe_advance<kStaged>(v, st, chunk, res, executed, rebases,
+      if (fe_advance<kStaged, kRawT>(v, st, chunk, res, executed, rebases,
                               v.trap ? v.trap + sid : nullptr)) {
         int r = 0, c = 0;
         sample_rc(v, sid, r, c);
@@ -190,10 +194,11 @@ __device__ __forceinline__ void fe_iter_warp(const DeviceView& v, const FePassBu
   }
 }
 
+template <bool kRawT>
 __global__ void __launch_bounds__(kPersistentThreads) fe_iter_kernel(DeviceView v,
                                                                        FePassBuffers b,
                                                                        RenderCtl ctl, int chunk) {
-  fe_iter_warp(v, b, ctl, chunk);
+  fe_iter_warp<false, kRawT>(v, b, ctl, chunk);
 }
 
 // The iteration pass with the FP64 rework overlapped: the last two warps of
@@ -220,7 +225,8 @@ __device__ __noinline__ void overlap_fp64_side(const DeviceView& v, const Overla
 
 // kStaged: the launch stages the orbit's first v.z_stage entries in its
 // dynamic shared memory (orbit_stage.cuh) and both sides read them there.
-template <bool kStaged>
+// kRawT: the FP32 step's t = 2Z + delta unnormalised (fe_core.cuh, kFeUTRaw).
+template <bool kStaged, bool kRawT>
 __global__ void __launch_bounds__(kPersistentThreads, 4) fe_overlap_kernel(
     DeviceView v, FePassBuffers b, RenderCtl ctl, OverlapCtl o, int chunk) {
   __shared__ SamplePool<typename Fp64AnyJobT<kStaged>::State> pool;
@@ -229,7 +235,7 @@ __global__ void __launch_bounds__(kPersistentThreads, 4) fe_overlap_kernel(
   const int warp = threadIdx.x >> 5;
   const int fe_warps = kPersistentThreads / 32 - kOverlapWarps;
   if (warp < fe_warps) {
-    fe_iter_warp<kStaged>(v, b, ctl, chunk);
+    fe_iter_warp<kStaged, kRawT>(v, b, ctl, chunk);
     producer_warp_done(o.fe_warps_done);
     return;
   }
@@ -261,14 +267,21 @@ void ensure_l2_set_aside(int device, size_t bytes) {
 
 int fe32_blocks_per_sm() {
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fe32_kernel, kPersistentThreads, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fe32_kernel<true>, kPersistentThreads, 0);
+  int per_sm_norm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_norm, fe32_kernel<false>,
+                                                kPersistentThreads, 0);
+  if (per_sm_norm < per_sm) per_sm = per_sm_norm;
   return per_sm;
 }
 
 cudaError_t launch_fe32(const DeviceView& v, const RenderCtl& ctl, cudaStream_t stream,
                         int blocks, int chunk) {
   note_launches(1);
-  fe32_kernel<<<blocks, kPersistentThreads, 0, stream>>>(v, ctl, chunk);
+  if (v.sa_fe)  // the arithmetic of the pass pipeline (launch_fe32_passes)
+    fe32_kernel<false><<<blocks, kPersistentThreads, 0, stream>>>(v, ctl, chunk);
+  else
+    fe32_kernel<true><<<blocks, kPersistentThreads, 0, stream>>>(v, ctl, chunk);
   return cudaGetLastError();
 }
 
@@ -289,8 +302,18 @@ cudaError_t launch_fe32_passes(const DeviceView& v, const FePassBuffers& b, cons
     DeviceView vs = v;
     vs.z_stage = z_stage < 0 ? 0 : (z_stage > v.zlen ? v.zlen : z_stage);
     const size_t dyn = 32 * (size_t)vs.z_stage;
-    const void* kernel = vs.z_stage > 0 ? (const void*)fe_overlap_kernel<true>
-                                        : (const void*)fe_overlap_kernel<false>;
+    // Views in the FP64 range take the unnormalised t (C2: 182 -> 170 ms); on
+    // floatexp views its larger bound reworks more samples, and their frame
+    // time is set by the reworked tail (1e-300 view: 31.3 -> 32.9 ms).
+    const bool raw_t = !v.sa_fe;
+    auto pick = [&](auto staged, auto raw) {
+      return fe_overlap_kernel<decltype(staged)::value, decltype(raw)::value>;
+    };
+    using T_ = std::true_type;
+    using F_ = std::false_type;
+    auto kfn = vs.z_stage > 0 ? (raw_t ? pick(T_{}, T_{}) : pick(T_{}, F_{}))
+                              : (raw_t ? pick(F_{}, T_{}) : pick(F_{}, F_{}));
+    const void* kernel = (const void*)kfn;
     if (dyn > 48 * 1024)
       cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
     const int oblocks =
@@ -316,15 +339,13 @@ cudaError_t launch_fe32_passes(const DeviceView& v, const FePassBuffers& b, cons
       cfg.attrs = attr;
       cfg.numAttrs = 1;
     }
-    cudaError_t e = vs.z_stage > 0
-                        ? cudaLaunchKernelEx(&cfg, fe_overlap_kernel<true>, vs, b, it, *overlap, chunk)
-                        : cudaLaunchKernelEx(&cfg, fe_overlap_kernel<false>, vs, b, it, *overlap,
-                                             chunk);
+    cudaError_t e = cudaLaunchKernelEx(&cfg, kfn, vs, b, it, *overlap, chunk);
     if (e != cudaSuccess) return e;
   } else {
+    auto kfn = v.sa_fe ? fe_iter_kernel<false> : fe_iter_kernel<true>;  // as the overlap kernel
     const int iblocks =
-        blocks > 0 ? blocks : blocks_for((const void*)fe_iter_kernel, kPersistentThreads, device);
-    fe_iter_kernel<<<iblocks, kPersistentThreads, 0, stream>>>(v, b, it, chunk);
+        blocks > 0 ? blocks : blocks_for((const void*)kfn, kPersistentThreads, device);
+    kfn<<<iblocks, kPersistentThreads, 0, stream>>>(v, b, it, chunk);
   }
   if (iter_end) cudaEventRecord(iter_end, stream);
   return cudaGetLastError();

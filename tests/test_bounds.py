@@ -172,6 +172,47 @@ def test_float_float_multiply_add_rounding_bound():
     assert worst > Q(1, 1000)  # not vacuous
 
 
+def _add_twice_raw(zh, zl, dh, dl):
+    """ff32.cuh's ff_add_twice_raw (t = 2Z + delta, not renormalised)."""
+    s = _fma(Q(2), zh, dh)
+    bb = _fma(Q(-2), zh, s)
+    e = _add(_fma(Q(2), zh, -_add(s, -bb)), _add(dh, -bb))
+    return s, _add(e, _fma(Q(2), zl, dl))
+
+
+def test_fe32_step_local_error_bound():
+    """One FE32 step's arithmetic, t = 2Z + delta unnormalised then the
+    float-float multiply-add, against (2Z + delta) delta + eps in exact
+    arithmetic: within (kFeUT - u_z) P' + u |eps|_1, P' = (2|Z.h|_1 + |delta.h|_1)
+    |delta.h|_1 (fe_core.cuh's derivation), also where 2Z + delta cancels."""
+    rng = np.random.default_rng(21)
+    k_t = Q(0x194, 256) * Q(1, 2 ** 43) - Q(1, 2 ** 45)  # kFeUT - u_z = 1.328125 * 2^-43
+    u = Q(9, 8) * Q(1, 2 ** 43)
+    worst = Q(0)
+    for _ in range(3000):
+        z = [_ffq(rng.uniform(-2, 2) * 10.0 ** rng.integers(-3, 1)) for _ in range(2)]
+        d = [_ffq(rng.uniform(-1, 1) * 10.0 ** rng.integers(-8, 1)) for _ in range(2)]
+        if rng.random() < 0.3:  # Y near -Z: t = 2Z + delta cancels
+            k = int(rng.integers(0, 2))
+            d[k] = _ffq(float(-2 * (z[k][0] + z[k][1])) * (1 + rng.uniform(-1e-6, 1e-6)))
+        ep = [_ffq(rng.uniform(-1, 1) * 10.0 ** rng.integers(-12, -2)) for _ in range(2)]
+        t = [_add_twice_raw(z[k][0], z[k][1], d[k][0], d[k][1]) for k in range(2)]
+        for k in range(2):  # |t.h| <= (2|Z.h| + |delta.h|)(1 + 2^-24)
+            assert abs(t[k][0]) <= (2 * abs(z[k][0]) + abs(d[k][0])) * (1 + Q(1, 2 ** 24))
+        (nr, ni) = _cmul_add(t[0], t[1], d[0], d[1], ep[0], ep[1])
+        T = [2 * (z[k][0] + z[k][1]) + d[k][0] + d[k][1] for k in range(2)]
+        D = [a[0] + a[1] for a in d]
+        E = [a[0] + a[1] for a in ep]
+        xr = T[0] * D[0] - T[1] * D[1] + E[0]
+        xi = T[0] * D[1] + T[1] * D[0] + E[1]
+        err = abs(nr[0] + nr[1] - xr) + abs(ni[0] + ni[1] - xi)
+        p = (2 * (abs(z[0][0]) + abs(z[1][0])) + abs(d[0][0]) + abs(d[1][0])) * (abs(d[0][0]) + abs(d[1][0]))
+        bound = k_t * p + u * (abs(ep[0][0]) + abs(ep[1][0]))
+        assert err <= bound
+        worst = max(worst, err / bound)
+    assert worst > Q(1, 1000)  # not vacuous
+
+
 def test_eps_below_the_double_range_is_below_half_an_ulp():
     """The plain FP64 step on floatexp views leaves out an eps component below
     2^-1022 (pixel_xd.cuh: plain_eps): exact because every sum it would be

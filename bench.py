@@ -139,9 +139,10 @@ def max_over_ranks(ms, device=None):
     return float(t.item())
 
 
-# FE32 step: 1.411e12 thread instructions for 1.209e10 steps, the iteration
-# kernel alone (--fe32-overlap 0) on the central 540x960-pixel crop (ncu)
-INSTR_PER_ITER = 116.7
+# FE32 step: 1.339e12 thread instructions for 1.209e10 steps, the iteration
+# kernel alone (--fe32-overlap 0) on the central 540x960-pixel crop (ncu,
+# smsp__thread_inst_executed.sum of fe_iter_kernel)
+INSTR_PER_ITER = 110.7
 
 
 def issue_roofline(executed, iter_ms, clocks):

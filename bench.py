@@ -796,9 +796,11 @@ def run_deep(args):
     precompute_s = time.perf_counter() - t0
     if args.profile:
         m.render()
-        print("profile case %dx%d, FE32: %.1f ms, rework %d, FP64 fronts %d" % (
-            nr, nc, m.stat(nm.STAT_KERNEL_NS) * 1e-6, m.stat(nm.STAT_FP64_REWORK),
-            m.stat(nm.STAT_FRONT_FP64)))
+        print("profile case %dx%d, FE32: %.1f ms (+ %.1f ms rework after the pass), rework %d, "
+              "FP64 fronts %d, executed FE32 steps %d" % (
+                  nr, nc, m.stat(nm.STAT_KERNEL_NS) * 1e-6, m.stat(nm.STAT_REWORK_KERNEL_NS) * 1e-6,
+                  m.stat(nm.STAT_FP64_REWORK), m.stat(nm.STAT_FRONT_FP64),
+                  m.stat(nm.STAT_EXECUTED_ITERS)))
         return
     for _ in range(args.warmup):
         m.render()

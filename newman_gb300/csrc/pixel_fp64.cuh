@@ -206,6 +206,32 @@ NM_HD bool above_bits(double r2, double bailout2) {
 #endif
 }
 
+// |yr|, |yi| < 2^8 (biased exponents below 1031): yr^2 + yi^2 then rounds to
+// at most 2^17, below the bailout radius squared (always 2^20 here), so the
+// bailout test is decided without forming it.
+NM_HD bool inside_bailout(double yr, double yi) {
+  return exp_field(yr) < 1031 && exp_field(yi) < 1031;
+}
+
+// The step's bailout and rebase tests in delta_steps' order and rounding, with
+// the FP64 operations of r2 = yr^2 + yi^2 and d2 = dr^2 + di^2 spent only where
+// the exponents leave the outcome open: 0 go on, 1 rebase, 2 escape (r2 set).
+NM_HD int bailout_and_rebase(double yr, double yi, double dr, double di, bool last,
+                             double bailout2, double& r2) {
+  const bool inside = inside_bailout(yr, yi);
+  if (!inside) {
+    r2 = add_(mul_(yr, yr), mul_(yi, yi));
+    if (above_bits(r2, bailout2)) return 2;
+  }
+  if (last) return 1;
+  if (clearly_larger(yr, yi, dr, di)) return 0;
+  // delta clearly larger (and of at least 2^-500, so that d2 is no underflow)
+  if (clearly_larger(dr, di, yr, yi) && (exp_field(dr) >= 523 || exp_field(di) >= 523)) return 1;
+  if (inside) r2 = add_(mul_(yr, yr), mul_(yi, yi));
+  return above_bits(add_(mul_(dr, dr), mul_(di, di)), r2) ? 1 : 0;
+}
+
+
 // The double loop's start at Z0 = descend(pt) (mandelbrot.cpp:234, 242).
 NM_HD void hw_start(Dbl2 px, Dbl2 py, HwState& st) {
   st.z0r = px.x;
@@ -458,17 +484,16 @@ NM_HD bool delta_steps(const DeviceView& v, DeltaState& st, int steps, EscapeVal
     j++;
     z = zn;
     double yr = add_(zn.x, dr), yi = add_(zn.y, di);
-    double r2 = add_(mul_(yr, yr), mul_(yi, yi));
-    if (above_bits(r2, v.bailout2)) {
+    // the bailout test r2 > 2^20, then the rebase test r2 < d2 (or the
+    // orbit's end), their FP64 sums formed only where exponents do not decide
+    double r2 = 0.0;
+    const int event = bailout_and_rebase(yr, yi, dr, di, j == zlast, v.bailout2, r2);
+    if (event == 2) {
       sm = smoothing_of(r2, v.log_bailout);
       out = {i, (float)sm};
       return true;
     }
-    // the rebase test r2 < d2, evaluated only when |Y| is not clearly larger
-    bool rebase = j == zlast;
-    if (!rebase && !clearly_larger(yr, yi, dr, di))
-      rebase = above_bits(add_(mul_(dr, dr), mul_(di, di)), r2);
-    if (rebase) {
+    if (event == 1) {
       dr = yr;
       di = yi;
       j = 0;

@@ -171,16 +171,14 @@ NM_HD bool delta_guarded_steps(const DeviceView& v, DeltaState& st, int steps, E
     di = nim;
     j++;
     z = zn;
-    const double r2 = add_(mul_(yr, yr), mul_(yi, yi));
-    if (above_bits(r2, v.bailout2)) {
+    double r2 = 0.0;
+    const int event = bailout_and_rebase(yr, yi, dr, di, j == zlast, v.bailout2, r2);
+    if (event == 2) {
       sm = smoothing_of(r2, v.log_bailout);
       out = {i, (float)sm};
       return true;
     }
-    bool rebase = j == zlast;
-    if (!rebase && !clearly_larger(yr, yi, dr, di))
-      rebase = above_bits(add_(mul_(dr, dr), mul_(di, di)), r2);
-    if (rebase) {
+    if (event == 1) {
       dr = yr;
       di = yi;
       j = 0;

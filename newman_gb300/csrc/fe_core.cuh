@@ -431,9 +431,17 @@ __device__ __forceinline__ bool fe_scaled_steps(const DeviceView& v, FeState& st
   const int start = st.i;
   ZFF z = fe_load_z<kStaged>(v, st.j);
   bool done = false;
+  // delta * 2^E as a float-float (0 below 2^-140, as in fe_renormalise's
+  // range): E stays fixed through these steps, and for -140 <= E the factor
+  // 2^E is a float (subnormal below 2^-126), so x * 2^E rounds once, exactly
+  // as ldexpf(x, E) does
+  const float sfac = st.E < -140 ? 0.0f
+                     : st.E >= -126 ? __int_as_float((st.E + 127) << 23)
+                                    : __int_as_float(1 << (st.E + 149));
+  auto unscaled = [&](FF d) { return FF{d.h * sfac, d.l * sfac}; };
   for (; st.i < stop; st.i++) {
-    const FF sd_r = st.E < -140 ? FF{0.f, 0.f} : ff_scale(st.dr, st.E);
-    const FF sd_i = st.E < -140 ? FF{0.f, 0.f} : ff_scale(st.di, st.E);
+    const FF sd_r = unscaled(st.dr);
+    const FF sd_i = unscaled(st.di);
     const FF tr = fe_twice_plus<kRawT>(z.hx, z.lx, sd_r);
     const FF ti = fe_twice_plus<kRawT>(z.hy, z.ly, sd_i);
     const float zl1 = up_add(fabsf(z.hx), fabsf(z.hy)), dl1 = up_add(fabsf(st.dr.h), fabsf(st.di.h));
@@ -454,9 +462,14 @@ __device__ __forceinline__ bool fe_scaled_steps(const DeviceView& v, FeState& st
     st.j++;
     z = fe_load_z<kStaged>(v, st.j);
     const float zm2 = fmaf(z.hx, z.hx, z.hy * z.hy);
-    const FF yr = ff_add(FF{z.hx, z.lx}, st.E < -140 ? FF{0.f, 0.f} : ff_scale(st.dr, st.E));
-    const FF yi = ff_add(FF{z.hy, z.ly}, st.E < -140 ? FF{0.f, 0.f} : ff_scale(st.di, st.E));
+    // Y = Z + delta, formed where it is used (the escape test, the rebase)
+    auto y_of = [&](FF& yr, FF& yi) {
+      yr = ff_add(FF{z.hx, z.lx}, unscaled(st.dr));
+      yi = ff_add(FF{z.hy, z.ly}, unscaled(st.di));
+    };
     if (zm2 > kFeBailout2 * (1.0f - 0x1p-10f)) {
+      FF yr, yi;
+      y_of(yr, yi);
       const float yerr = up_add(fmaxf(ldexpf(st.err, st.E), 0x1p-126f),
                                 up_mul(kFeUZ, up_add(fabsf(z.hx), fabsf(z.hy))));
       bool cert = st.certified != 0;
@@ -481,6 +494,8 @@ __device__ __forceinline__ bool fe_scaled_steps(const DeviceView& v, FeState& st
     if (st.j == zlast) {  // orbit exhausted: rebase to Z[0], now unscaled
       const float e_abs = up_add(up_add(fmaxf(ldexpf(st.err, st.E), 0x1p-126f), kFeUZ * 2048.0f),
                                  up_mul(kFeU, up_add(zl1, dmag)));
+      FF yr, yi;
+      y_of(yr, yi);
       st.dr = yr;
       st.di = yi;
       st.er = ff_scale(st.er, st.E);

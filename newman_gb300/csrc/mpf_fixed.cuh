@@ -299,6 +299,22 @@ MPF_HD Mpfx<P> mpf_add(const Mpfx<P>& a, const Mpfx<P>& b) {
   const Mpfx<P>& U = m > 0 ? a : b;
   const Mpfx<P>& W = m > 0 ? b : a;
   const int off = U.e - W.e;  // W's limb k sits at U's index k + off; off >= 0
+  {
+    // The common case: U's top limb exceeds W's limb at the same place by 2 or
+    // more, so no leading limbs cancel, no borrow chain forms and the window's
+    // top word stays at least 1 -- the window below is U's D limbs less W's
+    // (t = s0 = z = 0), with U's limbs at fixed indexes.
+    const uint64_t top = U.d[0] - (off == 0 ? W.d[0] : 0ull);
+    if (top >= 2) {
+      uint64_t br = 0;
+#pragma unroll
+      for (int i = D - 1; i >= 1; i--) o.d[i] = subb(U.d[i], limb_at(W.d, i - off), br);
+      o.d[0] = top - br;
+      o.e = U.e;
+      o.s = U.s;
+      return o;
+    }
+  }
   // first index where the limbs differ (equal exponents: equal leading limbs
   // cancel)
   int t = 0;
@@ -447,14 +463,24 @@ MPF_HD void mpf_orbit_step(const Mpfx<P>& xr, const Mpfx<P>& xi, const Mpfx<P>& 
 // bailedOut (mandelbrot.cpp:58-61): sqMag(descend(z)) > 1024^2 in doubles,
 // unfused.
 template <int P>
-MPF_HD bool mpf_bailed_out(const Mpfx<P>& re, const Mpfx<P>& im, double* r2_out = nullptr) {
+MPF_HD double mpf_sq_mag_d(const Mpfx<P>& re, const Mpfx<P>& im) {
   const double a = mpf_get_d(re), b = mpf_get_d(im);
 #if defined(__CUDA_ARCH__)
-  const double r2 = __dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b));
+  return __dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b));
 #else
   volatile double aa = a * a, bb = b * b;
-  const double r2 = aa + bb;
+  return aa + bb;
 #endif
+}
+// r2_out, when given, is set where the test returns true.  Components below
+// 701 in magnitude (zero, a limb exponent of at most 0, or an integer limb of
+// at most 700) decide it without the doubles: get_d truncates toward zero, so
+// both doubles are at most 701 and r2 <= 2 * 701^2 (1 + 2^-52)^2 < 2^20.
+template <int P>
+MPF_HD bool mpf_bailed_out(const Mpfx<P>& re, const Mpfx<P>& im, double* r2_out = nullptr) {
+  auto small = [](const Mpfx<P>& x) { return x.s == 0 || x.e <= 0 || (x.e == 1 && x.d[0] <= 700); };
+  if (small(re) && small(im)) return false;
+  const double r2 = mpf_sq_mag_d(re, im);
   if (r2_out) *r2_out = r2;
   return r2 > 1024.0 * 1024.0;
 }

@@ -91,8 +91,7 @@ struct MpJob {
         mid = (low + high) / 2;
       }
       x_plus_d<P>(v, found, sa_value(v, found, eps, eps2, eps3), st.yr, st.yi);
-      double r2 = 0.0;
-      mpf_bailed_out(st.yr, st.yi, &r2);
+      const double r2 = mpf_sq_mag_d(st.yr, st.yi);
       sm = smoothing_of(r2, v.log_bailout);
       out = {found, (float)sm};
       return true;

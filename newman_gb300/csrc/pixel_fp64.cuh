@@ -273,11 +273,16 @@ NM_HD bool hw_steps(const DeviceView& v, HwState& st, int steps, EscapeValue& ou
     zi = nim;
     sr = mul_(zr, zr);
     si = mul_(zi, zi);
-    const double r2 = add_(sr, si);
-    if (above_bits(r2, v.bailout2)) {
-      sm = smoothing_of(r2, v.log_bailout);
-      out = {it, (float)sm};
-      return true;
+    // both squares below 2^19 (biased exponents under 1042): their sum rounds
+    // to at most 2^20, which does not bail out (bailout2 = 2^20); the sum is
+    // formed only where it can
+    if (exp_field(sr) >= 1042 || exp_field(si) >= 1042) {
+      const double r2 = add_(sr, si);
+      if (above_bits(r2, v.bailout2)) {
+        sm = smoothing_of(r2, v.log_bailout);
+        out = {it, (float)sm};
+        return true;
+      }
     }
     if (same_bits(zr, cr) && same_bits(zi, ci)) {
       cycle = true;

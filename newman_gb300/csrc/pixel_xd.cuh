@@ -45,18 +45,30 @@ NM_HD bool delta_xd_steps(const DeviceView& v, DeltaXDState& st, int steps, Esca
     j++;
     z = zn;
     const XD yr = xd_add(xd_of(zn.x), dr), yi = xd_add(xd_of(zn.y), di);
-    const XD r2 = xd_add(xd_mul(yr, yr), xd_mul(yi, yi));
-    if (xd_gt(r2, bail2)) {
-      sm = smoothing_of(xd_to_double(r2), v.log_bailout);
-      out = {i, (float)sm};
-      return true;
-    }
-    // the rebase test r2 < d2, evaluated only when |Y| is not clearly larger
-    // (larger component of Y at least 4 times delta's: |Y|^2 > 2 |delta|^2)
-    bool rebase = j == zlast;
+    // components of Y below 2^8: r2 < 2^17 does not bail out (bail2 = 2^20);
+    // r2 is formed only where a test needs it (delta_steps' bailout_and_rebase)
     const int32_t ey = yr.e > yi.e ? yr.e : yi.e, ed = dr.e > di.e ? dr.e : di.e;
-    if (!rebase && !(ey >= ed + 2 && (yr.m != 0.0 || yi.m != 0.0)))
-      rebase = xd_gt(xd_add(xd_mul(dr, dr), xd_mul(di, di)), r2);
+    const bool inside = ey < 8;
+    XD r2 = XD{0.0, kXdZeroExp};
+    if (!inside) {
+      r2 = xd_add(xd_mul(yr, yr), xd_mul(yi, yi));
+      if (xd_gt(r2, bail2)) {
+        sm = smoothing_of(xd_to_double(r2), v.log_bailout);
+        out = {i, (float)sm};
+        return true;
+      }
+    }
+    // the rebase test r2 < d2, decided by exponents where one of Y and delta
+    // is at least 4 times the other (|Y|^2 > 2 |delta|^2 or the reverse)
+    bool rebase = j == zlast;
+    if (!rebase && !(ey >= ed + 2 && (yr.m != 0.0 || yi.m != 0.0))) {
+      if (ed >= ey + 2 && (dr.m != 0.0 || di.m != 0.0)) {
+        rebase = true;
+      } else {
+        if (inside) r2 = xd_add(xd_mul(yr, yr), xd_mul(yi, yi));
+        rebase = xd_gt(xd_add(xd_mul(dr, dr), xd_mul(di, di)), r2);
+      }
+    }
     if (rebase) {
       dr = yr;
       di = yi;

@@ -210,8 +210,11 @@ __global__ void __launch_bounds__(kPersistentThreads) fe_iter_kernel(DeviceView 
 // Capped at 64 registers so that 4 blocks fit on an SM.  On the 1920x1080
 // (4x4 samples) view of width 1e-12, N 50,000 (2.7 % of the samples
 // reworked): 191 ms with two FP64 warps a block, 245 ms with one, 221 ms with
-// three, 243 ms with the rework after the pass.
-constexpr int kOverlapWarps = 2;
+// three, 243 ms with the rework after the pass.  Views whose FP64 side is the
+// longer one take three (fp64_warps_for): the 1e-300 view 31.3 -> 29.3 ms,
+// a 3840x2160 (2x2) view of width 1e-412 with N 2,000,000 1,317 -> 1,175 ms,
+// against 170 -> 182 ms on the 1e-12 view above.
+int fp64_warps_for(const DeviceView& v) { return (v.sa_fe || v.N > 200000) ? 3 : 2; }
 
 // The FP64 side, out of line: its register pressure (the FP64 series front)
 // then stays out of the FP32 iteration's allocation.
@@ -226,14 +229,15 @@ __device__ __noinline__ void overlap_fp64_side(const DeviceView& v, const Overla
 // kStaged: the launch stages the orbit's first v.z_stage entries in its
 // dynamic shared memory (orbit_stage.cuh) and both sides read them there.
 // kRawT: the FP32 step's t = 2Z + delta unnormalised (fe_core.cuh, kFeUTRaw).
-template <bool kStaged, bool kRawT>
+// kFp64Warps: the warps of a block on the FP64 side.
+template <bool kStaged, bool kRawT, int kFp64Warps>
 __global__ void __launch_bounds__(kPersistentThreads, 4) fe_overlap_kernel(
     DeviceView v, FePassBuffers b, RenderCtl ctl, OverlapCtl o, int chunk) {
   __shared__ SamplePool<typename Fp64AnyJobT<kStaged>::State> pool;
   if (kStaged) stage_orbit_prefix(v, ctl.stats + STAT_STAGE_FALLBACKS);
   pool_init(&pool);
   const int warp = threadIdx.x >> 5;
-  const int fe_warps = kPersistentThreads / 32 - kOverlapWarps;
+  const int fe_warps = kPersistentThreads / 32 - kFp64Warps;
   if (warp < fe_warps) {
     fe_iter_warp<kStaged, kRawT>(v, b, ctl, chunk);
     producer_warp_done(o.fe_warps_done);
@@ -306,8 +310,10 @@ cudaError_t launch_fe32_passes(const DeviceView& v, const FePassBuffers& b, cons
     // floatexp views its larger bound reworks more samples, and their frame
     // time is set by the reworked tail (1e-300 view: 31.3 -> 32.9 ms).
     const bool raw_t = !v.sa_fe;
+    const bool three = fp64_warps_for(v) == 3;
     auto pick = [&](auto staged, auto raw) {
-      return fe_overlap_kernel<decltype(staged)::value, decltype(raw)::value>;
+      return three ? fe_overlap_kernel<decltype(staged)::value, decltype(raw)::value, 3>
+                   : fe_overlap_kernel<decltype(staged)::value, decltype(raw)::value, 2>;
     };
     using T_ = std::true_type;
     using F_ = std::false_type;

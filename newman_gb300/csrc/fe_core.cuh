@@ -66,6 +66,12 @@ constexpr float kFeUT = 0x1.61p-43f;
 // (|Z| + |delta|) times the carried bound's own local term, inside the 2^-20
 // margin on |Y| in the amplification.
 constexpr float kFeUTRaw = 0x1.94p-43f;
+// Which t a view's FE32 steps take, the same in every kernel (a frame of a
+// batch and the frame rendered alone give the same bits): unnormalised on
+// views inside the FP64 range; floatexp views keep the renormalised t, whose
+// smaller bound reworks fewer samples, and their frame time follows the
+// reworked ones.
+NM_HD bool fe_raw_t(const DeviceView& v) { return !v.sa_fe; }
 // t = 2Z + delta for the step's multiply-add, renormalised or not.
 template <bool kRawT>
 __device__ __forceinline__ FF fe_twice_plus(float ah, float al, FF b) {

@@ -137,8 +137,8 @@ __device__ __forceinline__ void batch_iter_warp(const BatchGroup& grp, const FeP
       // the arithmetic of the frame rendered alone (render_fe32.cu): t = 2Z +
       // delta unnormalised on frames inside the FP64 range
       FeTrap* trap = v.trap ? v.trap + (g - grp.offsets[f]) : nullptr;
-      if (v.sa_fe ? fe_advance<false, false>(v, st, chunk, res, executed, rebases, trap)
-                  : fe_advance<false, true>(v, st, chunk, res, executed, rebases, trap)) {
+      if (fe_raw_t(v) ? fe_advance<false, true>(v, st, chunk, res, executed, rebases, trap)
+                      : fe_advance<false, false>(v, st, chunk, res, executed, rebases, trap)) {
         int r = 0, c = 0;
         sample_rc(v, g - grp.offsets[f], r, c);
         log_cost(v, r, c, executed - exec0, 1);

@@ -282,7 +282,7 @@ int fe32_blocks_per_sm() {
 cudaError_t launch_fe32(const DeviceView& v, const RenderCtl& ctl, cudaStream_t stream,
                         int blocks, int chunk) {
   note_launches(1);
-  if (v.sa_fe)  // the arithmetic of the pass pipeline (launch_fe32_passes)
+  if (!fe_raw_t(v))  // the arithmetic of the pass pipeline (launch_fe32_passes)
     fe32_kernel<false><<<blocks, kPersistentThreads, 0, stream>>>(v, ctl, chunk);
   else
     fe32_kernel<true><<<blocks, kPersistentThreads, 0, stream>>>(v, ctl, chunk);
@@ -309,7 +309,7 @@ cudaError_t launch_fe32_passes(const DeviceView& v, const FePassBuffers& b, cons
     // Views in the FP64 range take the unnormalised t (C2: 182 -> 170 ms); on
     // floatexp views its larger bound reworks more samples, and their frame
     // time is set by the reworked tail (1e-300 view: 31.3 -> 32.9 ms).
-    const bool raw_t = !v.sa_fe;
+    const bool raw_t = fe_raw_t(v);
     const bool three = fp64_warps_for(v) == 3;
     auto pick = [&](auto staged, auto raw) {
       return three ? fe_overlap_kernel<decltype(staged)::value, decltype(raw)::value, 3>
@@ -348,7 +348,7 @@ cudaError_t launch_fe32_passes(const DeviceView& v, const FePassBuffers& b, cons
     cudaError_t e = cudaLaunchKernelEx(&cfg, kfn, vs, b, it, *overlap, chunk);
     if (e != cudaSuccess) return e;
   } else {
-    auto kfn = v.sa_fe ? fe_iter_kernel<false> : fe_iter_kernel<true>;  // as the overlap kernel
+    auto kfn = fe_raw_t(v) ? fe_iter_kernel<true> : fe_iter_kernel<false>;  // as the overlap kernel
     const int iblocks =
         blocks > 0 ? blocks : blocks_for((const void*)kfn, kPersistentThreads, device);
     kfn<<<iblocks, kPersistentThreads, 0, stream>>>(v, b, it, chunk);

@@ -1,9 +1,10 @@
 // newman oracle -- TEST INFRASTRUCTURE ONLY.
 //
 // A CPU restatement of newman's per-pixel Mandelbrot path (mandelbrot.cpp,
-// complex.h, grid.h of axnjaxn/newman), used by the tests, the smoke check and
-// the CPU-baseline leg of the benchmark as the checker.  Nothing in the
-// product (newman_gb300/) links, loads or calls this file.
+// complex.h, grid.h of axnjaxn/newman), used by the tests and the smoke check
+// to compare the GPU results against, and timed as the benchmark's CPU
+// baseline.  Nothing in the product (newman_gb300/) links, loads or calls this
+// file.
 //
 // Parity status: PARITY UNPINNED.  The reference ships no tests, golden
 // vectors or fixtures, and it cannot be compiled here (gmpxx.h / gmp.h,

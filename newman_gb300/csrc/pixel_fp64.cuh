@@ -213,6 +213,16 @@ NM_HD bool inside_bailout(double yr, double yi) {
   return exp_field(yr) < 1031 && exp_field(yi) < 1031;
 }
 
+// Both tests decided before Y = Z + delta is formed: every component of Z and
+// of delta below 2^7 (so |Y|'s components stay below 2^8: no bailout), and Z's
+// larger component at least 8 times delta's (so Y's larger component is at
+// least 4 times delta's: clearly_larger, no rebase).  Not at the orbit's end.
+NM_HD bool no_event_before_y(Dbl2 zn, double dr, double di) {
+  const int zr = exp_field(zn.x), zi = exp_field(zn.y), ar = exp_field(dr), ai = exp_field(di);
+  const int ez = zr > zi ? zr : zi, ed = ar > ai ? ar : ai;
+  return ez < 1030 && ed < 1030 && ez >= ed + 3;
+}
+
 // The step's bailout and rebase tests in delta_steps' order and rounding, with
 // the FP64 operations of r2 = yr^2 + yi^2 and d2 = dr^2 + di^2 spent only where
 // the exponents leave the outcome open: 0 go on, 1 rebase, 2 escape (r2 set).
@@ -488,11 +498,16 @@ NM_HD bool delta_steps(const DeviceView& v, DeltaState& st, int steps, EscapeVal
     di = nim;
     j++;
     z = zn;
-    double yr = add_(zn.x, dr), yi = add_(zn.y, di);
     // the bailout test r2 > 2^20, then the rebase test r2 < d2 (or the
-    // orbit's end), their FP64 sums formed only where exponents do not decide
-    double r2 = 0.0;
-    const int event = bailout_and_rebase(yr, yi, dr, di, j == zlast, v.bailout2, r2);
+    // orbit's end), with Y and the FP64 sums formed only where exponents do
+    // not decide
+    double yr = 0.0, yi = 0.0, r2 = 0.0;
+    int event = 0;
+    if (j == zlast || !no_event_before_y(zn, dr, di)) {
+      yr = add_(zn.x, dr);
+      yi = add_(zn.y, di);
+      event = bailout_and_rebase(yr, yi, dr, di, j == zlast, v.bailout2, r2);
+    }
     if (event == 2) {
       sm = smoothing_of(r2, v.log_bailout);
       out = {i, (float)sm};

@@ -170,11 +170,18 @@ NM_HD bool delta_guarded_steps(const DeviceView& v, DeltaState& st, int steps, E
     const double ti = add_(twice_(z.y), di);
     const double nre = add_(sub_(mul_(tr, dr), mul_(ti, di)), st.er);
     const double nim = add_(add_(mul_(tr, di), mul_(ti, dr)), st.ei);
-    const double yr = add_(zn.x, nre), yi = add_(zn.y, nim);
+    // Y = Z + delta only where the tests need it (delta_steps); a Y that is
+    // not formed feeds nothing, so only the formed values are guarded
+    const bool need_y = j + 1 == zlast || !no_event_before_y(zn, nre, nim);
+    double yr = 0.0, yi = 0.0;
+    if (need_y) {
+      yr = add_(zn.x, nre);
+      yi = add_(zn.y, nim);
+    }
     // (with eps below the double range its components were not added: exact
     // unless a sum came out 0)
     if (near_underflow(tr) || near_underflow(ti) || near_underflow(nre) || near_underflow(nim) ||
-        near_underflow(yr) || near_underflow(yi) ||
+        (need_y && (near_underflow(yr) || near_underflow(yi))) ||
         (eps_tiny && ((xd_bits_(nre) << 1) == 0 || (xd_bits_(nim) << 1) == 0))) {
       handover = true;  // state (dr, di, j, i) is before this step
       break;
@@ -184,7 +191,8 @@ NM_HD bool delta_guarded_steps(const DeviceView& v, DeltaState& st, int steps, E
     j++;
     z = zn;
     double r2 = 0.0;
-    const int event = bailout_and_rebase(yr, yi, dr, di, j == zlast, v.bailout2, r2);
+    const int event =
+        need_y ? bailout_and_rebase(yr, yi, dr, di, j == zlast, v.bailout2, r2) : 0;
     if (event == 2) {
       sm = smoothing_of(r2, v.log_bailout);
       out = {i, (float)sm};

@@ -223,6 +223,41 @@ NM_HD bool no_event_before_y(Dbl2 zn, double dr, double di) {
   return ez < 1030 && ed < 1030 && ez >= ed + 3;
 }
 
+// |x| as a float from the double's high word: its exponent rebiased and the
+// top 20 of its 52 mantissa bits, so within 2^-20 below |x|.  For biased
+// exponents in [963, 1083] (|x| in [2^-60, 2^61)), where the float and the
+// squares below stay normal.
+NM_HD float abs_hi_float(double x) {
+#if defined(__CUDA_ARCH__)
+  const unsigned hi = (unsigned)__double2hiint(x) & 0x7fffffffu;
+  return __uint_as_float((hi - ((1023u - 127u) << 20)) << 3);
+#else
+  unsigned long long b;
+  std::memcpy(&b, &x, 8);
+  const unsigned hi = (unsigned)(b >> 32) & 0x7fffffffu;
+  const unsigned f = (hi - ((1023u - 127u) << 20)) << 3;
+  float r;
+  std::memcpy(&r, &f, 4);
+  return r;
+#endif
+}
+
+// The rebase test (FP64 d2 > r2) decided on FP32 estimates where they lie far
+// apart, else -1.  Each estimate is within 2^-18 of its exact value (operands
+// within 2^-20 below, two FP32 roundings) and each FP64 sum within 2^-51, so a
+// ratio beyond 1 + 2^-15 between the estimates orders the FP64 values too.
+NM_HD int rebase_by_estimate(double yr, double yi, double dr, double di) {
+  const int a = exp_field(yr), b = exp_field(yi), c = exp_field(dr), d = exp_field(di);
+  const int lo = min(min(a, b), min(c, d)), hi = max(max(a, b), max(c, d));
+  if (lo < 963 || hi > 1083) return -1;
+  const float yrf = abs_hi_float(yr), yif = abs_hi_float(yi);
+  const float drf = abs_hi_float(dr), dif = abs_hi_float(di);
+  const float r2f = fmaf(yrf, yrf, yif * yif), d2f = fmaf(drf, drf, dif * dif);
+  if (d2f > r2f * (1.0f + 0x1p-15f)) return 1;
+  if (r2f > d2f * (1.0f + 0x1p-15f)) return 0;
+  return -1;
+}
+
 // The step's bailout and rebase tests in delta_steps' order and rounding, with
 // the FP64 operations of r2 = yr^2 + yi^2 and d2 = dr^2 + di^2 spent only where
 // the exponents leave the outcome open: 0 go on, 1 rebase, 2 escape (r2 set).
@@ -237,6 +272,8 @@ NM_HD int bailout_and_rebase(double yr, double yi, double dr, double di, bool la
   if (clearly_larger(yr, yi, dr, di)) return 0;
   // delta clearly larger (and of at least 2^-500, so that d2 is no underflow)
   if (clearly_larger(dr, di, yr, yi) && (exp_field(dr) >= 523 || exp_field(di) >= 523)) return 1;
+  const int q = rebase_by_estimate(yr, yi, dr, di);
+  if (q >= 0) return q;
   if (inside) r2 = add_(mul_(yr, yr), mul_(yi, yi));
   return above_bits(add_(mul_(dr, dr), mul_(di, di)), r2) ? 1 : 0;
 }

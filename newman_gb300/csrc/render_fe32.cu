@@ -213,7 +213,8 @@ __global__ void __launch_bounds__(kPersistentThreads) fe_iter_kernel(DeviceView 
 // three, 243 ms with the rework after the pass.  Views whose FP64 side is the
 // longer one take three (fp64_warps_for): the 1e-300 view 31.3 -> 29.3 ms,
 // a 3840x2160 (2x2) view of width 1e-412 with N 2,000,000 1,317 -> 1,175 ms,
-// against 170 -> 182 ms on the 1e-12 view above.
+// against 170 -> 182 ms on the 1e-12 view above; four are slower on both deep
+// views (31.3 and 1,350 ms).
 int fp64_warps_for(const DeviceView& v) { return (v.sa_fe || v.N > 200000) ? 3 : 2; }
 
 // The FP64 side, out of line: its register pressure (the FP64 series front)

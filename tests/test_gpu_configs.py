@@ -186,8 +186,7 @@ def test_c3_learned_order_gain(nm):
     own renders logged on C1, C2 and C3 (32x32-pixel tiles), then orders C3's
     tiles from a capped preview on the GPU (nm_order_tiles).  The render in
     that order is bit-identical to the static order's, and in this test's runs
-    shorter; the
-    recorded times give the gain with and without the preview (measured:
+    shorter; the recorded times give the gain with and without the preview (measured:
     render 34.0 -> 29.9, 30.6 -> 27.8 and 28.4 -> 25.3 ms, order by the true
     costs 28.8, 28.0 and 24.7 ms, preview and ordering ~3 ms)."""
     import time

@@ -248,8 +248,8 @@ NM_HD float abs_hi_float(double x) {
 // ratio beyond 1 + 2^-15 between the estimates orders the FP64 values too.
 NM_HD int rebase_by_estimate(double yr, double yi, double dr, double di) {
   const int a = exp_field(yr), b = exp_field(yi), c = exp_field(dr), d = exp_field(di);
-  const int lo = min(min(a, b), min(c, d)), hi = max(max(a, b), max(c, d));
-  if (lo < 963 || hi > 1083) return -1;
+  const int lo1 = a < b ? a : b, lo2 = c < d ? c : d, hi1 = a > b ? a : b, hi2 = c > d ? c : d;
+  if ((lo1 < lo2 ? lo1 : lo2) < 963 || (hi1 > hi2 ? hi1 : hi2) > 1083) return -1;
   const float yrf = abs_hi_float(yr), yif = abs_hi_float(yi);
   const float drf = abs_hi_float(dr), dif = abs_hi_float(di);
   const float r2f = fmaf(yrf, yrf, yif * yif), d2f = fmaf(drf, drf, dif * dif);

@@ -1,13 +1,11 @@
-// Pipe-throughput probes: the FP32 and FP64 issue ceilings that the
-// per-sample kernels are measured against (the roofline denominators).
+// Pipe-throughput probes for bench.py: the FP32 and FP64 issue ceilings that
+// the per-sample kernels are measured against (the roofline denominators).
+// Not part of the library; bench.py builds it into _bench_build/ and loads it
+// with ctypes.
 //
 // Each thread runs 8 independent dependency chains of one instruction kind,
 // on every SM, long enough (~100 ms) that launch overhead is negligible.
 #include <cuda_runtime.h>
-
-#include "engine.hpp"
-
-#include "newman_gb300.h"
 
 namespace {
 
@@ -56,13 +54,15 @@ __global__ void muladd64_kernel(double* out, int iters, double a, double b) {
 
 }  // namespace
 
-extern "C" int nm_peak_flops(int kind, double* flops_per_s) {
-  if (!flops_per_s || kind < 0 || kind > 2) return NM_ERR_ARG;
+// kind 0: FP32 FMA, 1: FP64 FMA, 2: FP64 unfused multiply + add; flop/s into
+// *flops_per_s.  0 on success, 1 for bad arguments, 2 for a CUDA error.
+extern "C" int bench_peak_flops(int kind, double* flops_per_s) {
+  if (!flops_per_s || kind < 0 || kind > 2) return 1;
   int dev = 0, sms = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) return NM_ERR_CUDA;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 2;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   void* buf = nullptr;
-  if (cudaMalloc(&buf, 64) != cudaSuccess) return NM_ERR_CUDA;
+  if (cudaMalloc(&buf, 64) != cudaSuccess) return 2;
   const int threads = 256, blocks = sms * 8;
   const int iters = kind == 0 ? 1 << 19 : 1 << 13;
   cudaEvent_t e0, e1;
@@ -71,7 +71,6 @@ extern "C" int nm_peak_flops(int kind, double* flops_per_s) {
   float best_ms = 1e30f;
   for (int rep = 0; rep < 4; rep++) {
     cudaEventRecord(e0);
-    nmg::note_launches(1);
     if (kind == 0)
       fma32_kernel<<<blocks, threads>>>((float*)buf, iters, 0.999999f, 1e-6f);
     else if (kind == 1)
@@ -88,9 +87,9 @@ extern "C" int nm_peak_flops(int kind, double* flops_per_s) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaFree(buf);
-  if (err != cudaSuccess) return NM_ERR_CUDA;
+  if (err != cudaSuccess) return 2;
   const double insts = (double)blocks * threads * iters * kChains;
   const double flops = insts * 2.0;  // one FMA, or one multiply plus one add
   *flops_per_s = flops / (best_ms * 1e-3);
-  return NM_OK;
+  return 0;
 }

@@ -332,11 +332,6 @@ int nm_batch_autotune(nm_batch* b, int stride, int* tile_w, int* tile_h, int* re
 #define NM_NOALLOC_MAX_SAMPLES 4194304
 int nm_render_fe32_noalloc(nm_handle* h, nm_escape_value* out, void* stream);
 
-/* Measured issue ceiling of the current GPU, in flop/s (no reference
-   counterpart; the roofline denominator of the per-sample kernels).
-   kind 0: FP32 FMA, 1: FP64 FMA, 2: FP64 unfused multiply + add. */
-int nm_peak_flops(int kind, double* flops_per_s);
-
 #ifdef __cplusplus
 }
 #endif

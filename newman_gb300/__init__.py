@@ -40,7 +40,7 @@ EXPORTS = (
     "nm_upload", "nm_get_orbit", "nm_compute_row", "nm_render_rows", "nm_render", "nm_synchronize", "nm_cancel",
     "nm_at", "nm_at_sc", "nm_scale_up", "nm_scale_down", "nm_reduce", "nm_get_grid",
     "nm_get_smoothing64", "nm_device_grid", "nm_point_at", "nm_translate", "nm_zoom",
-    "nm_zoom_at", "nm_load_legacy", "nm_save", "nm_peak_flops", "nm_render_fe32_noalloc",
+    "nm_zoom_at", "nm_load_legacy", "nm_save", "nm_render_fe32_noalloc",
     "nm_batch_create", "nm_batch_destroy", "nm_batch_add", "nm_batch_set_option",
     "nm_batch_render", "nm_batch_get_stat", "nm_batch_frames", "nm_batch_autotune",
     "nm_preview", "nm_tiles", "nm_set_tile_order", "nm_get_tile_costs", "nm_tile_features",
@@ -114,7 +114,6 @@ def load_library(path=LIB_PATH):
         "nm_zoom_at": (i32, [vp, ctypes.c_float, i32, i32, i32]),
         "nm_load_legacy": (i32, [vp, cp]),
         "nm_save": (i32, [vp, cp]),
-        "nm_peak_flops": (i32, [i32, P(dbl)]),
         "nm_render_fe32_noalloc": (i32, [vp, vp, vp]),
         "nm_batch_create": (vp, [i32]),
         "nm_batch_destroy": (None, [vp]),
@@ -304,13 +303,6 @@ class CostModel:
         _check(_lib.nm_cost_model_train(self._m, x.ctypes.data, t.ctypes.data, len(x),
                                         int(epochs), float(lr), ctypes.byref(loss)))
         return loss.value
-
-
-def peak_flops(kind):
-    """Measured FP32 FMA (0), FP64 FMA (1) or FP64 unfused (2) flop/s."""
-    v = ctypes.c_double(0.0)
-    _check(load_library().nm_peak_flops(int(kind), ctypes.byref(v)))
-    return v.value
 
 
 class Mandelbrot:

@@ -540,8 +540,14 @@ int nm_order_tiles(nm_handle* h, nm_handle* preview, nm_costmodel* m) {
   if (int rc = nmg::ensure_device(h)) return rc;
   cudaStream_t s = h->stream;
   // after the preview's render, and after the model's own pending work
-  cudaEvent_t ev = nullptr;
-  NM_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  struct Event {  // destroyed on every return
+    cudaEvent_t e = nullptr;
+    ~Event() {
+      if (e) cudaEventDestroy(e);
+    }
+  } event;
+  NM_CUDA(cudaEventCreateWithFlags(&event.e, cudaEventDisableTiming));
+  cudaEvent_t ev = event.e;
   NM_CUDA(cudaEventRecord(ev, preview->render_stream ? preview->render_stream : preview->stream));
   NM_CUDA(cudaStreamWaitEvent(s, ev, 0));
   NM_CUDA(cudaEventRecord(ev, m->stream));
@@ -572,7 +578,6 @@ int nm_order_tiles(nm_handle* h, nm_handle* preview, nm_costmodel* m) {
   // the model's next calls (which reuse x and y) wait for the sort
   NM_CUDA(cudaEventRecord(ev, s));
   NM_CUDA(cudaStreamWaitEvent(m->stream, ev, 0));
-  NM_CUDA(cudaEventDestroy(ev));
   h->tile_order.clear();
   h->tile_order_on_device = true;
   h->tile_order_n = ntiles;

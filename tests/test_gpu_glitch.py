@@ -65,3 +65,6 @@ def test_rebasing_leaves_no_glitch(nm, oracle_mod, k):
         bad = grids[path] != ref
         assert bad.mean() <= 0.01, (path, bad.mean())
         assert _largest_blob(bad) <= 3, path
+    # and the FE32 path (on these views inside the FP64 range: t = 2Z + delta
+    # unnormalised, kFeUTRaw) certifies every count it keeps: the FP64 path's
+    assert (grids["PATH_FE32"] == grids["PATH_FP64"]).mean() >= 0.9999
